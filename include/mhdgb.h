@@ -1,0 +1,163 @@
+/*
+ * mhdgb.h -- C ABI of the GB300 ideal-MHD solver step (libmhdgb.so).
+ *
+ * One handle = one grid on one CUDA device, with its own stream.  The library owns all device
+ * memory; callers pass host arrays in the reference's FieldArray layout
+ * (src_cpp_kokkos_host/mhd.hpp:186-245: element (n,k,j,i) at i + itot*(n + nv*(j + jtot*k)),
+ * itot = nx + 2*ngh + 1, ngh = 2, src_cpp_kokkos_host/config.hpp:53-59).
+ * Every function returns MHDGB_OK (0) or a negative status; mhdgb_last_error() gives the text.
+ * A handle is not thread safe; different handles are independent.
+ *
+ * Three groups of entry points:
+ *  - stage entry points, one per reference stage function (hydflux_mod / boundary_mod), which run
+ *    the FP64 stage kernels on the handle's U / P / Fx,Fy,Fz arrays with the reference's rounding
+ *    (bit-for-bit equal to the reference's CPU build);
+ *  - the fused step (mhdgb_step / mhdgb_run_until): the whole main-loop body of
+ *    src_cpp_kokkos_host/main.cpp:229-259 as one persistent kernel per step, CUDA-graph captured,
+ *    in the FP64 form or the FP32-mixed form;
+ *  - the ensemble: many independent grids of uneven size advanced together.
+ */
+#ifndef MHDGB_H_
+#define MHDGB_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MHDGB_OK 0
+#define MHDGB_ERR_ARG (-1)        /* invalid argument / configuration */
+#define MHDGB_ERR_CUDA (-2)       /* CUDA runtime or driver error */
+#define MHDGB_ERR_NONFINITE (-3)  /* a non-finite dt / c_h candidate was produced */
+#define MHDGB_ERR_NEGATIVE (-4)   /* rho <= 0 or p <= 0 in some cell */
+#define MHDGB_ERR_TIMEOUT (-5)    /* a bounded device-side wait gave up */
+#define MHDGB_ERR_STATE (-6)      /* call out of order (e.g. no state uploaded) */
+#define MHDGB_ERR_NOMEM (-7)      /* device allocation failed */
+
+/* boundary types, src_cpp_kokkos_host/config.hpp:29-31 */
+#define MHDGB_BC_PERIODIC 1
+#define MHDGB_BC_REFLECTION 2
+#define MHDGB_BC_OUTFLOW 3
+
+/* precision of the fused step */
+#define MHDGB_FP64 0        /* FP64 throughout, FMA contraction (last-bit differences) */
+#define MHDGB_FP64_EXACT 1  /* FP64, separately rounded: bit-for-bit the reference's arithmetic */
+#define MHDGB_MIXED 2       /* FP32 reconstruction + Riemann solve; FP64 state, update, pressure
+                               recovery and reductions */
+
+#define MHDGB_NPRIM 12 /* hydflux_mod::nprim, mhd.hpp:320 */
+#define MHDGB_NCONS 10 /* hydflux_mod::mconsv, mhd.hpp:325 */
+
+/* Compile-time parameters of src_cpp_kokkos_host/config.hpp:10-42 (one rank) plus hydflux_mod::gam
+ * (mhd.cpp:27) and the CFL factor hard-coded at mhd.cpp:1560, as run-time values. */
+typedef struct mhdgb_config {
+  int nx, ny, nz;                  /* config::ngridtotal1..3 (interior cells) */
+  double x1min, x1max, x2min, x2max, x3min, x3max; /* config::x?min / x?max */
+  int bc[6];                       /* boundary_xin, _xout, _yin, _yout, _zin, _zout */
+  double gam;                      /* hydflux_mod::gam */
+  double cfl;                      /* dt = cfl * min_cells(...); the reference uses 0.05 */
+  int precision;                   /* MHDGB_FP64, MHDGB_FP64_EXACT or MHDGB_MIXED */
+  int spacing_quirk;               /* 1: UpdateConservU takes the y/z spacing at index i as
+                                      mhd.cpp:1435-1436 does (requires nx <= ny, nx <= nz) */
+  int device;                      /* CUDA device ordinal */
+} mhdgb_config;
+
+typedef struct mhdgb_solver mhdgb_solver;
+
+/* Progress of the fused step (read by mhdgb_sync). */
+typedef struct mhdgb_report {
+  long long step;   /* fused steps completed */
+  double time;      /* resolution_mod::time_sim */
+  double dt;        /* dt of the latest step */
+  double chg;       /* c_h of the latest step */
+  double next_dt;   /* dt the next step will use */
+  double next_chg;  /* c_h the next step will use */
+  int done;         /* time > tmax or step >= max_steps reached */
+  unsigned status;  /* device status bits: 1 non-finite, 2 non-positive rho/p, 4 wait timeout */
+} mhdgb_report;
+
+/* Defaults of src_cpp_kokkos_host/config.hpp (150^3, KH domain and boundaries) with gam = 5/3. */
+int mhdgb_config_default(mhdgb_config* cfg);
+
+/* AllocateHydroVariables + AllocateBoundaryVariables (mhd.cpp:33-77, boundary.cpp:36-95) and
+ * GenerateGrid (main.cpp:26-65). */
+int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out);
+/* DeallocateHydroVariables / DeallocateBoundaryVariables (mhd.cpp:79-87, boundary.cpp:98-104). */
+int mhdgb_destroy(mhdgb_solver* h);
+const char* mhdgb_last_error(const mhdgb_solver* h);
+const char* mhdgb_status_string(int status);
+/* itot, jtot, ktot of the handle (resolution_mod, config.hpp:57-59). */
+int mhdgb_extents(const mhdgb_solver* h, int* itot, int* jtot, int* ktot);
+/* Bytes of device memory held by the handle. */
+size_t mhdgb_device_bytes(const mhdgb_solver* h);
+
+/* GridArray G (mhd.hpp:22-182): cell faces x1a/x2a/x3a, lengths itot/jtot/ktot. */
+int mhdgb_get_grid(const mhdgb_solver* h, double* x1a, double* x2a, double* x3a);
+int mhdgb_set_grid(mhdgb_solver* h, const double* x1a, const double* x2a, const double* x3a);
+
+/* State transfer (FieldArray::h2d / d2h, mhd.hpp:310-315).  U: 10 fields, P: 12 fields, F: 10. */
+int mhdgb_upload_cons(mhdgb_solver* h, const double* U);
+int mhdgb_upload_prim(mhdgb_solver* h, const double* P);
+int mhdgb_download_cons(mhdgb_solver* h, double* U);
+int mhdgb_download_prim(mhdgb_solver* h, double* P);
+int mhdgb_download_flux(mhdgb_solver* h, int dir, double* F);
+
+/* ---- stage entry points (synchronous, FP64, reference rounding) ---- */
+/* ControlTimestep (mhd.cpp:1511-1561): dt = cfl * min over the interior; sets the handle's dt. */
+int mhdgb_control_timestep(mhdgb_solver* h, double* dt);
+/* SetBoundaryCondition (boundary.cpp:750-893) with the single-rank SendRecvBoundary fills. */
+int mhdgb_set_boundary(mhdgb_solver* h);
+/* EvaluateCh (mhd.cpp:1563-1611): sets the handle's chg. */
+int mhdgb_evaluate_ch(mhdgb_solver* h, double* chg);
+/* GetNumericalFluxD(dir) (mhd.cpp:987-1410), dir = 1, 2, 3: fills Fx, Fy or Fz. */
+int mhdgb_flux(mhdgb_solver* h, int dir);
+/* UpdateConservU (mhd.cpp:1412-1444). */
+int mhdgb_update_conserv(mhdgb_solver* h);
+/* DampPsi (mhd.cpp:1613-1633). */
+int mhdgb_damp_psi(mhdgb_solver* h);
+/* UpdatePrimitvP (mhd.cpp:1447-1509). */
+int mhdgb_update_prim(mhdgb_solver* h);
+/* resolution_mod::dt (config.hpp:49) and hydflux_mod::chg (mhd.cpp:26) of the stage path. */
+int mhdgb_set_dt(mhdgb_solver* h, double dt);
+int mhdgb_set_chg(mhdgb_solver* h, double chg);
+
+/* ---- fused step ---- */
+/* Recover P from U (UpdatePrimitvP over the interior, mhd.cpp:1480-1507), fill the ghosts and
+ * reduce the first step's dt and c_h; called implicitly by the first mhdgb_step after an upload. */
+int mhdgb_prepare(mhdgb_solver* h);
+/* Enqueue nsteps steps of the main loop (main.cpp:229-259) on the handle's stream; returns
+ * without waiting.  Steps after the stop condition (see mhdgb_set_stop) do nothing. */
+int mhdgb_step(mhdgb_solver* h, int nsteps);
+/* Stop condition of the loop, main.cpp:265: time > tmax or step >= max_steps. */
+int mhdgb_set_stop(mhdgb_solver* h, double tmax, long long max_steps);
+/* Run until the stop condition holds; report may be NULL. */
+int mhdgb_run_until(mhdgb_solver* h, double tmax, long long max_steps, mhdgb_report* report);
+/* Wait for the enqueued steps and report progress; returns a status for device-side errors. */
+int mhdgb_sync(mhdgb_solver* h, mhdgb_report* report);
+/* Reset time and step counters (resolution_mod::time_sim = 0). */
+int mhdgb_reset_clock(mhdgb_solver* h);
+/* One step on caller-owned host arrays: upload U (10 fields, reference layout), run nsteps fused
+ * steps, download the new U and return the step's dt and c_h.  The drop-in form of the loop body
+ * for callers that keep the state on the host. */
+int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nsteps, double* dt, double* chg);
+
+/* Time nsteps fused steps with CUDA events recorded on the handle's stream around the enqueued
+ * launches (synchronising before and after); *ms receives the elapsed device time. */
+int mhdgb_time_steps(mhdgb_solver* h, int nsteps, double* ms);
+
+/* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):
+ * out = {volume, <X(1-X)>, sqrt(<v_y^2>)} over the interior, FP64 sums. */
+int mhdgb_diag(mhdgb_solver* h, double out[3]);
+
+/* Kelvin-Helmholtz initial state (single shear layer v_x = vshear*tanh(y/width), rho = 1, p = 1,
+ * B = (bx,0,0), v_y = amp*sin(2 pi x) exp(-(y/sig)^2) + noise*(2u-1) with u seeded per cell,
+ * scalar X = (1+tanh(y/width))/2) written into U; see mhdturbulence_gb300/ic.py. */
+int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, double width, double bx, double amp,
+                  double sig, double noise);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

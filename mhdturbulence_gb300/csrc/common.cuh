@@ -1,0 +1,164 @@
+// common.cuh -- device layout, the per-solver control block and the inline-PTX helpers (mbarrier,
+// TMA tensor loads) shared by the solver kernels.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mhd_defs.cuh"
+
+namespace mhdgb {
+
+constexpr int NGH = 2;  // ghost layers, src_cpp_kokkos_host/config.hpp:56
+
+// Device arrays use the reference FieldArray layout (src_cpp_kokkos_host/mhd.hpp:237-238,
+// View(n1,nv,n2,n3) LayoutLeft: i fastest, then variable, then j, then k) with the i extent
+// padded from itot = nx+2*ngh+1 to a pitch `ip` that makes every row 64-byte aligned (TMA needs
+// 16-byte strides).  Index space is the reference's: cell i of the interior is i + ngh.
+struct Layout {
+  int nx, ny, nz;     // interior cells
+  int itot, jtot, ktot;
+  int ip;             // padded i pitch (elements)
+  __host__ __device__ size_t at(int nv, int n, int k, int j, int i) const {
+    return (size_t)i + (size_t)ip * ((size_t)n + (size_t)nv * ((size_t)j + (size_t)jtot * (size_t)k));
+  }
+  __host__ __device__ size_t count(int nv) const { return (size_t)ip * nv * jtot * ktot; }
+};
+
+// Status bits of the device status word (checked by the host at synchronisation points).
+enum : unsigned { ST_NONFINITE = 1u, ST_NEGATIVE = 2u, ST_TIMEOUT = 4u, ST_TMA = 8u };
+
+// Reduction slot: min of the per-cell CFL time and max of the per-cell signal speed, kept as the
+// bit patterns of non-negative doubles (which order like unsigned integers).
+struct RedSlot {
+  unsigned long long dtmin_bits;
+  unsigned long long chmax_bits;
+};
+
+// Per-solver control block in device memory.  Fused steps read the current step's dt and c_h
+// from slot[step % 3], reduce the next step's values into slot[(step+1) % 3] and reset
+// slot[(step+2) % 3]; the last CTA to finish advances step and time.
+struct Ctrl {
+  RedSlot slot[3];
+  unsigned long long step;   // fused steps completed
+  double time;               // accumulated simulated time (time_sim)
+  double tmax;               // stop when time > tmax (the reference's main.cpp:265 test)
+  unsigned long long max_step;
+  unsigned done;             // set once time > tmax or step >= max_step: later steps do nothing
+  unsigned status;           // ST_* bits
+  unsigned blocks_done;      // CTA completion counter of the running launch
+  unsigned work_next;        // dynamic tile queue head of the running launch
+  double last_dt, last_ch;   // dt and c_h used by the latest completed step
+};
+
+__host__ __device__ inline unsigned long long dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  union { double d; unsigned long long u; } v; v.d = x; return v.u;
+#endif
+}
+__host__ __device__ inline double bitsd(unsigned long long u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  union { double d; unsigned long long u; } v; v.u = u; return v.d;
+#endif
+}
+constexpr unsigned long long DT_RESET = 0x7FEFFFFFFFFFFFFFull;  // DBL_MAX
+constexpr unsigned long long CH_RESET = 0x0ull;                 // +0.0
+
+// ---------------------------------------------------------------------------------------------
+// Block reductions of (min dt, max ch) with a non-finite check, then one atomic per CTA.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void warp_minmax(double& mn, double& mx) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double a = __shfl_xor_sync(0xffffffffu, mn, o);
+    double b = __shfl_xor_sync(0xffffffffu, mx, o);
+    mn = smin(mn, a);
+    mx = smax(mx, b);
+  }
+}
+
+// All threads of the block must call.  scratch: >= 2*32 doubles of shared memory.
+__device__ __forceinline__ void block_reduce_to_slot(double mn, double mx, double* scratch, RedSlot* slot) {
+  warp_minmax(mn, mx);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) { scratch[wid] = mn; scratch[32 + wid] = mx; }
+  __syncthreads();
+  if (wid == 0) {
+    mn = (lane < nw) ? scratch[lane] : 1.0e308;
+    mx = (lane < nw) ? scratch[32 + lane] : 0.0;
+    warp_minmax(mn, mx);
+    if (lane == 0) {
+      atomicMin(&slot->dtmin_bits, dbits(mn));
+      atomicMax(&slot->chmax_bits, dbits(mx));
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------------------------
+// mbarrier + TMA (cp.async.bulk.tensor) helpers.  Waits are bounded: on timeout the waiter sets
+// ST_TIMEOUT in the status word and gives up instead of spinning forever.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Returns false (and flags ST_TIMEOUT) if the phase did not complete within the spin budget.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* status) {
+  for (unsigned it = 0; it < (1u << 24); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 64) __nanosleep(32);
+  }
+  atomicOr(status, ST_TIMEOUT);
+  return false;
+}
+
+// 4-D tiled TMA load of one box into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_4d(void* smem_dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            int c3, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(smem_dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
+}
+
+}  // namespace mhdgb

@@ -1,0 +1,49 @@
+// kernels.h -- host-side launchers of the device kernels (implemented in stages.cu / fast.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "fused_args.h"
+
+namespace mhdgb {
+
+// ---- stage kernels (stages.cu, FP64, separately rounded) ----
+cudaError_t launch_flux(int dir, const double* P, double* F, const Layout& L, const double* chg, cudaStream_t s);
+cudaError_t launch_update_conserv(const double* Fx, const double* Fy, const double* Fz, double* U, const Layout& L,
+                                  const double* xinv, const double* yinv, const double* zinv, int quirk,
+                                  const double* dt, cudaStream_t s);
+cudaError_t launch_damp_psi(double* U, const Layout& L, const double* dxs, const double* dys, const double* dzs,
+                            const double* dt, const double* chg, cudaStream_t s);
+cudaError_t launch_update_prim(const double* U, double* P, const Layout& L, double gam, cudaStream_t s);
+cudaError_t launch_reduce_dt_ch(const double* P, const Layout& L, const double* dxs, const double* dys,
+                                const double* dzs, RedSlot* slot, unsigned* status, int nsm, cudaStream_t s);
+cudaError_t launch_reset_slot(RedSlot* slot, cudaStream_t s);
+cudaError_t launch_slot_to_scalars(const RedSlot* slot, double cfl, double* dt, double* ch, cudaStream_t s);
+size_t pack_buffer_doubles(const Layout& L);
+cudaError_t launch_ghost_fill(double* P, const Layout& L, const int bc[6], double* scratch, cudaStream_t s);
+
+// ---- fused step (stages.cu: FP64 bit-exact; fast.cu: FP64 and mixed with FMA contraction) ----
+FusedShape fused_shape(FusedKind kind);
+// Sets the kernel attributes (dynamic shared memory); call once per device before launching.
+cudaError_t fused_prepare(FusedKind kind);
+// Occupancy: CTAs of the fused kernel resident per SM.
+int fused_ctas_per_sm(FusedKind kind);
+cudaError_t launch_fused(FusedKind kind, const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s);
+// Recover P (FP64 for FP64 kinds, FP32 for mixed) + ghost images from U; reduce dt/c_h into slot.
+cudaError_t launch_recover(FusedKind kind, const double* U, void* P, const Layout& L, const int bc[6],
+                           const double* dxs, const double* dys, const double* dzs, double gam, RedSlot* slot,
+                           unsigned* status, int nsm, cudaStream_t s);
+
+namespace detail {  // the bit-exact FP64 instantiation, compiled in stages.cu
+FusedShape exact_shape();
+cudaError_t exact_prepare();
+int exact_ctas_per_sm();
+cudaError_t exact_launch(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s);
+cudaError_t exact_recover(const double* U, void* P, const Layout& L, const int bc[6], const double* dxs,
+                          const double* dys, const double* dzs, double gam, RedSlot* slot, unsigned* status,
+                          int nsm, cudaStream_t s);
+}  // namespace detail
+
+}  // namespace mhdgb

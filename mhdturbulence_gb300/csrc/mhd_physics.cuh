@@ -1,0 +1,316 @@
+// mhd_physics.cuh -- per-face physics of the ideal-MHD step, as device functions templated on the
+// arithmetic type R (double for the FP64 form, float for the mixed form's reconstruction and
+// Riemann solve).
+//
+// Every expression keeps the operation order of the reference's src_cpp_kokkos_host/mhd.cpp
+// (left-to-right evaluation of the C++ source).  Compiled with -fmad=false the FP64 instantiation
+// therefore reproduces the reference's separately rounded results bit for bit; compiled with FMA
+// contraction it differs from them in the last bits only.  The two builds live in different
+// translation units; MHDGB_VNS names the namespace of the current one so that their instantiations
+// never merge at link time.
+#pragma once
+
+#include "mhd_defs.cuh"
+
+#ifndef MHDGB_VNS
+#error "define MHDGB_VNS (v_exact or v_fast) before including mhd_physics.cuh"
+#endif
+
+namespace mhdgb {
+namespace MHDGB_VNS {
+
+// vanLeer, src_cpp_kokkos_host/mhd.cpp:89-95.  The limited slope of a cell c is
+// van_leer(P[c+1]-P[c], P[c]-P[c-1]); the reference evaluates the same expression for the left
+// state of face c+1/2 and the right state of face c-1/2 (mhd.cpp:1134-1154), so one evaluation
+// per cell and direction gives both.
+template <class R>
+__device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
+  return (dsvp * dsvm > R(0)) ? R(2) * dsvp * dsvm / (dsvp + dsvm) : R(0);
+}
+
+// Rotation maps of Prim2Cons1/2/3, mhd.cpp:1078-1118.
+template <int DIR> struct Dir;
+template <> struct Dir<1> {
+  static constexpr int muv1 = muvu, muv2 = muvv, muv3 = muvw, mub1 = mubu, mub2 = mubv, mub3 = mubw;
+  static constexpr int mfv1 = mfvu, mfv2 = mfvv, mfv3 = mfvw;
+  static constexpr int nved = nve1, nbmd = nbm1, nvef = nve2, nbmf = nbm2, nveb = nve3, nbmb = nbm3;
+  // output slots, mhd.cpp:1225-1240
+  static constexpr int orv1 = mrvu, orv2 = mrvv, orv3 = mrvw, glm = mbm1;
+  static constexpr int ob_a = mbm2, sb_a = mubv, ob_b = mbm3, sb_b = mubw;
+};
+template <> struct Dir<2> {
+  static constexpr int muv1 = muvw, muv2 = muvu, muv3 = muvv, mub1 = mubw, mub2 = mubu, mub3 = mubv;
+  static constexpr int mfv1 = mfvw, mfv2 = mfvu, mfv3 = mfvv;
+  static constexpr int nved = nve2, nbmd = nbm2, nvef = nve3, nbmf = nbm3, nveb = nve1, nbmb = nbm1;
+  // mhd.cpp:1306-1321
+  static constexpr int orv1 = mrvw, orv2 = mrvu, orv3 = mrvv, glm = mbm2;
+  static constexpr int ob_a = mbm1, sb_a = mubw, ob_b = mbm3, sb_b = mubv;
+};
+template <> struct Dir<3> {
+  static constexpr int muv1 = muvv, muv2 = muvw, muv3 = muvu, mub1 = mubv, mub2 = mubw, mub3 = mubu;
+  static constexpr int mfv1 = mfvv, mfv2 = mfvw, mfv3 = mfvu;
+  static constexpr int nved = nve3, nbmd = nbm3, nvef = nve1, nbmf = nbm1, nveb = nve2, nbmb = nbm2;
+  // mhd.cpp:1391-1406
+  static constexpr int orv1 = mrvv, orv2 = mrvw, orv3 = mrvu, glm = mbm3;
+  static constexpr int ob_a = mbm1, sb_a = mubv, ob_b = mbm2, sb_b = mubw;
+};
+
+// Prim2ConsD, mhd.cpp:997-1076 (note the energy flux term bsq*B_d of mhd.cpp:1049-1050).
+template <class R, int DIR>
+__device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
+  using D = Dir<DIR>;
+  const R rho = Prim[nden];
+  const R rhoinv = R(1) / rho;
+  const R vsq = Prim[nve1] * Prim[nve1] + Prim[nve2] * Prim[nve2] + Prim[nve3] * Prim[nve3];
+  const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
+  Cons[mudn] = rho;
+  Cons[D::muv1] = rho * Prim[nve1];
+  Cons[D::muv2] = rho * Prim[nve2];
+  Cons[D::muv3] = rho * Prim[nve3];
+  Cons[muet] = rho * Prim[nene] + R(0.5) * rho * vsq + R(0.5) * bsq;
+  Cons[D::mub1] = Prim[nbm1];
+  Cons[D::mub2] = Prim[nbm2];
+  Cons[D::mub3] = Prim[nbm3];
+  Cons[mubp] = Prim[nbps];
+  Cons[must] = rho * Prim[nst];
+  const R ptl = Prim[npre] + bsq / R(2);
+  Cons[mfdn] = rho * Prim[D::nved];
+  Cons[D::mfv1] = rho * Prim[nve1] * Prim[D::nved] - Prim[nbm1] * Prim[D::nbmd];
+  Cons[D::mfv2] = rho * Prim[nve2] * Prim[D::nved] - Prim[nbm2] * Prim[D::nbmd];
+  Cons[D::mfv3] = rho * Prim[nve3] * Prim[D::nved] - Prim[nbm3] * Prim[D::nbmd];
+  Cons[mfet] = (Cons[muet] + ptl) * Prim[D::nved] - bsq * Prim[D::nbmd];
+  Cons[mfvu] += ptl;
+  Cons[mfbu] = R(0);
+  Cons[mfbv] = Prim[D::nbmf] * Prim[D::nved] - Prim[D::nvef] * Prim[D::nbmd];
+  Cons[mfbw] = Prim[D::nbmb] * Prim[D::nved] - Prim[D::nveb] * Prim[D::nbmd];
+  Cons[mfbp] = R(0);
+  Cons[mfst] = rho * Prim[nst] * Prim[D::nved];
+  const R css = Prim[ncsp] * Prim[ncsp];
+  const R cts = css + bsq * rhoinv;
+  Cons[mcsp] = sqrt((cts + sqrt(cts * cts - R(4) * css * Prim[D::nbmd] * Prim[D::nbmd] * rhoinv)) / R(2));
+  Cons[mvel] = Prim[D::nved];
+  Cons[mpre] = ptl;
+}
+
+// HLLD, mhd.cpp:97-417.  Writes the 10 rotated fluxes (slot mubp is left undefined: the GLM pair
+// replaces it).
+template <class R>
+__device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], R (&nflux)[NCONS]) {
+  const R eps = R(1.0e-30);
+  const R rol = leftst[mudn], eel = leftst[muet];
+  const R rxl = leftst[muvu], ryl = leftst[muvv], rzl = leftst[muvw];
+  const R vxl = leftst[muvu] / leftst[mudn];
+  const R vyl = leftst[muvv] / leftst[mudn];
+  const R vzl = leftst[muvw] / leftst[mudn];
+  const R byl = leftst[mubv], bzl = leftst[mubw], ptl = leftst[mpre], scl = leftst[must];
+  const R ror = rigtst[mudn], eer = rigtst[muet];
+  const R rxr = rigtst[muvu], ryr = rigtst[muvv], rzr = rigtst[muvw];
+  const R vxr = rigtst[muvu] / rigtst[mudn];
+  const R vyr = rigtst[muvv] / rigtst[mudn];
+  const R vzr = rigtst[muvw] / rigtst[mudn];
+  const R byr = rigtst[mubv], bzr = rigtst[mubw], ptr = rigtst[mpre], scr = rigtst[must];
+
+  // Step 1 (mhd.cpp:212-216)
+  const R cfl = leftst[mcsp], cfr = rigtst[mcsp];
+  const R sl = smin(vxl, vxr) - smax(cfl, cfr);
+  const R sr = smax(vxl, vxr) + smax(cfl, cfr);
+  // Step 2 (mhd.cpp:221-243)
+  const R frol = leftst[mfdn], feel = leftst[mfet], frxl = leftst[mfvu], fryl = leftst[mfvv];
+  const R frzl = leftst[mfvw], fbyl = leftst[mfbv], fbzl = leftst[mfbw], fscl = leftst[mfst];
+  const R fror = rigtst[mfdn], feer = rigtst[mfet], frxr = rigtst[mfvu], fryr = rigtst[mfvv];
+  const R frzr = rigtst[mfvw], fbyr = rigtst[mfbv], fbzr = rigtst[mfbw], fscr = rigtst[mfst];
+  // Step 4 (mhd.cpp:248-258)
+  const R sdl = smin(R(-1e-20), sl - vxl);
+  const R sdr = smax(R(1e-20), sr - vxr);
+  const R rosdl = rol * sdl;
+  const R rosdr = ror * sdr;
+  R temp = R(1) / (rosdr - rosdl);
+  const R sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * temp;
+  const R sdml = smin(R(-1e-20), sl - sm);
+  const R isdml = R(1) / sdml;
+  const R sdmr = smax(R(1e-20), sr - sm);
+  const R isdmr = R(1) / sdmr;
+  // Step 5 (mhd.cpp:264)
+  const R ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * temp;
+  // Step 5A (mhd.cpp:269-300)
+  const R bxs = R(0.5) * (leftst[mubu] + rigtst[mubu]);
+  const R bxsq = bxs * bxs;
+  R temp_fst = rosdl * sdml - bxsq;
+  R sign1 = copysign(R(1), fabs(temp_fst) - eps);
+  R maxs1 = smax(R(0), sign1);
+  R mins1 = smin(R(0), sign1);
+  R itf = R(1) / (temp_fst + mins1);
+  temp = bxs * (sdl - sdml) * itf;
+  const R rolst = maxs1 * (rosdl * isdml) - mins1 * rol;
+  const R sclst = rolst / rol * scl;
+  const R vxlst = maxs1 * sm - mins1 * vxl;
+  const R rxlst = rolst * vxlst;
+  const R vylst = maxs1 * (vyl - byl * temp) - mins1 * vyl;
+  const R rylst = rolst * vylst;
+  const R vzlst = maxs1 * (vzl - bzl * temp) - mins1 * vzl;
+  const R rzlst = rolst * vzlst;
+  temp = (rosdl * sdl - bxsq) * itf;
+  const R bylst = maxs1 * (byl * temp) - mins1 * byl;
+  const R bzlst = maxs1 * (bzl * temp) - mins1 * bzl;
+  const R vdbstl = vxlst * bxs + vylst * bylst + vzlst * bzlst;
+  const R eelst = maxs1 * (sdl * eel - ptl * vxl + ptst * sm +
+                           bxs * (vxl * bxs + vyl * byl + vzl * bzl - vdbstl)) * isdml
+                  - mins1 * eel;
+  // Step 5B (mhd.cpp:305-333)
+  temp_fst = rosdr * sdmr - bxsq;
+  sign1 = copysign(R(1), fabs(temp_fst) - eps);
+  maxs1 = smax(R(0), sign1);
+  mins1 = smin(R(0), sign1);
+  itf = R(1) / (temp_fst + mins1);
+  temp = bxs * (sdr - sdmr) * itf;
+  const R rorst = maxs1 * (rosdr * isdmr) - mins1 * ror;
+  const R scrst = rorst / ror * scr;
+  const R vxrst = maxs1 * sm - mins1 * vxr;
+  const R rxrst = rorst * vxrst;
+  const R vyrst = maxs1 * (vyr - byr * temp) - mins1 * vyr;
+  const R ryrst = rorst * vyrst;
+  const R vzrst = maxs1 * (vzr - bzr * temp) - mins1 * vzr;
+  const R rzrst = rorst * vzrst;
+  temp = (rosdr * sdr - bxsq) * itf;
+  const R byrst = maxs1 * (byr * temp) - mins1 * byr;
+  const R bzrst = maxs1 * (bzr * temp) - mins1 * bzr;
+  const R vdbstr = vxrst * bxs + vyrst * byrst + vzrst * bzrst;
+  const R eerst = maxs1 * ((sdr * eer - ptr * vxr + ptst * sm) * isdmr +
+                           bxs * (vxr * bxs + vyr * byr + vzr * bzr - vdbstr) * isdmr)
+                  - mins1 * eer;
+  // Step 5C (mhd.cpp:338-377)
+  const R sqrtrol = sqrt(rolst);
+  const R sqrtror = sqrt(rorst);
+  const R abbx = fabs(bxs);
+  const R signbx = copysign(R(1), bxs);
+  sign1 = copysign(R(1), abbx - eps);
+  maxs1 = smax(R(0), sign1);
+  mins1 = -smin(R(0), sign1);
+  const R invsumro = maxs1 / (sqrtrol + sqrtror);
+  temp = invsumro * (sqrtrol * vylst + sqrtror * vyrst + signbx * (byrst - bylst));
+  const R vyldst = vylst * mins1 + temp;
+  const R ryldst = rylst * mins1 + rolst * temp;
+  const R ryrdst = ryrst * mins1 + rorst * temp;
+  temp = invsumro * (sqrtrol * vzlst + sqrtror * vzrst + signbx * (bzrst - bzlst));
+  const R vzldst = vzlst * mins1 + temp;
+  const R rzldst = rzlst * mins1 + rolst * temp;
+  const R rzrdst = rzrst * mins1 + rorst * temp;
+  temp = invsumro * (sqrtrol * byrst + sqrtror * bylst + signbx * sqrtrol * sqrtror * (vyrst - vylst));
+  const R byldst = bylst * mins1 + temp;
+  const R byrdst = byrst * mins1 + temp;
+  temp = invsumro * (sqrtrol * bzrst + sqrtror * bzlst + signbx * sqrtrol * sqrtror * (vzrst - vzlst));
+  const R bzldst = bzlst * mins1 + temp;
+  const R bzrdst = bzrst * mins1 + temp;
+  temp = sm * bxs + vyldst * byldst + vzldst * bzldst;
+  const R eeldst = eelst - sqrtrol * signbx * (vdbstl - temp) * maxs1;
+  const R eerdst = eerst + sqrtror * signbx * (vdbstr - temp) * maxs1;
+  // Step 6 (mhd.cpp:381-415)
+  const R slst = (sm - abbx / sqrtrol) * maxs1;
+  const R srst = (sm + abbx / sqrtror) * maxs1;
+  sign1 = copysign(R(1), sm);
+  maxs1 = smax(R(0), sign1);
+  mins1 = -smin(R(0), sign1);
+  const R msl = smin(sl, R(0));
+  const R msr = smax(sr, R(0));
+  const R mslst = smin(slst, R(0));
+  const R msrst = smax(srst, R(0));
+  nflux[mden] = (frol + (rolst - rol) * msl) * maxs1 + (fror + (rorst - ror) * msr) * mins1;
+  nflux[meto] = (feel + (eelst - eel) * msl + (eeldst - eelst) * mslst) * maxs1
+              + (feer + (eerst - eer) * msr + (eerdst - eerst) * msrst) * mins1;
+  nflux[mrv1] = (frxl + (rxlst - rxl) * msl) * maxs1 + (frxr + (rxrst - rxr) * msr) * mins1;
+  nflux[mrv2] = (fryl + (rylst - ryl) * msl + (ryldst - rylst) * mslst) * maxs1
+              + (fryr + (ryrst - ryr) * msr + (ryrdst - ryrst) * msrst) * mins1;
+  nflux[mrv3] = (frzl + (rzlst - rzl) * msl + (rzldst - rzlst) * mslst) * maxs1
+              + (frzr + (rzrst - rzr) * msr + (rzrdst - rzrst) * msrst) * mins1;
+  nflux[mbm1] = R(0);
+  nflux[mbm2] = (fbyl + (bylst - byl) * msl + (byldst - bylst) * mslst) * maxs1
+              + (fbyr + (byrst - byr) * msr + (byrdst - byrst) * msrst) * mins1;
+  nflux[mbm3] = (fbzl + (bzlst - bzl) * msl + (bzldst - bzlst) * mslst) * maxs1
+              + (fbzr + (bzrst - bzr) * msr + (bzrdst - bzrst) * msrst) * mins1;
+  nflux[mst] = (fscl + (sclst - scl) * msl) * maxs1 + (fscr + (scrst - scr) * msr) * mins1;
+  nflux[mbps] = R(0);
+}
+
+// Face flux from the reconstructed left/right primitive states: Prim2Cons of both sides, HLLD,
+// then the rotation back to (rho, m1, m2, m3, E, B1, B2, B3, psi, X) order with the GLM pair for
+// the normal field and psi (mhd.cpp:1223-1240 and equivalents).
+template <class R, int DIR>
+__device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NPRIM], R chg, R (&F)[NCONS]) {
+  using D = Dir<DIR>;
+  R Cl[NVEC], Cr[NVEC], nf[NCONS];
+  prim2cons<R, DIR>(Pl, Cl);
+  prim2cons<R, DIR>(Pr, Cr);
+  hlld<R>(Cl, Cr, nf);
+  F[mden] = nf[mden];
+  F[mrv1] = nf[D::orv1];
+  F[mrv2] = nf[D::orv2];
+  F[mrv3] = nf[D::orv3];
+  F[meto] = nf[meto];
+  // HLLD output slots for the two tangential fields (numflux[mbmv]/[mbmw] = slots 6/7)
+  F[D::ob_a] = nf[D::sb_a];
+  F[D::ob_b] = nf[D::sb_b];
+  F[D::glm] = R(0.5) * (Cl[mubp] + Cr[mubp]) - R(0.5) * chg * (Cr[mubu] - Cl[mubu]);
+  F[mbps] = (R(0.5) * (Cl[mubu] + Cr[mubu]) - R(0.5) / chg * (Cr[mubp] - Cl[mubp])) * chg * chg;
+  F[mst] = nf[mst];
+}
+
+// Left state of face c+1/2 and right state of face c-1/2 from cell value p and limited slope s
+// (mhd.cpp:1139 and 1153).
+template <class R> __device__ __forceinline__ R left_state(R p, R s) { return p + R(0.5) * s; }
+template <class R> __device__ __forceinline__ R right_state(R p, R s) { return p - R(0.5) * s; }
+
+// UpdatePrimitvP for one cell, mhd.cpp:1483-1506.  u: 10 conserved values -> p: 12 primitives.
+template <class R>
+__device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPRIM]) {
+  const R rho = u[mden];
+  const R rhoinv = R(1) / rho;
+  p[nden] = rho;
+  p[nve1] = u[mrv1] * rhoinv;
+  p[nve2] = u[mrv2] * rhoinv;
+  p[nve3] = u[mrv3] * rhoinv;
+  const R ekin = R(0.5) * (u[mrv1] * u[mrv1] + u[mrv2] * u[mrv2] + u[mrv3] * u[mrv3]) * rhoinv;
+  const R emag = R(0.5) * (u[mbm1] * u[mbm1] + u[mbm2] * u[mbm2] + u[mbm3] * u[mbm3]);
+  p[nene] = (u[meto] - ekin - emag) / u[mden];
+  p[npre] = p[nene] * p[nden] * (gam - R(1));
+  p[ncsp] = sqrt(p[nene] * gam * (gam - R(1)));
+  p[nbm1] = u[mbm1];
+  p[nbm2] = u[mbm2];
+  p[nbm3] = u[mbm3];
+  p[nbps] = u[mbps];
+  p[nst] = u[mst] * rhoinv;
+}
+
+// Per-cell CFL time (ControlTimestep, mhd.cpp:1542-1550): min over d of dx_d/(|v_d| + ctot).
+template <class R>
+__device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
+  const R ctot = sqrt(p[ncsp] * p[ncsp] + (p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3]) / p[nden]);
+  R dt = dx / (fabs(p[nve1]) + ctot);
+  const R b = dy / (fabs(p[nve2]) + ctot);
+  const R c = dz / (fabs(p[nve3]) + ctot);
+  if (b < dt) dt = b;
+  if (c < dt) dt = c;
+  return dt;
+}
+
+// Per-cell maximum signal speed (EvaluateCh, mhd.cpp:1589-1601).
+template <class R>
+__device__ __forceinline__ R cell_ch(const R (&p)[NPRIM]) {
+  const R css = p[ncsp] * p[ncsp];
+  const R ca1 = p[nbm1] * p[nbm1] / p[nden];
+  const R ca2 = p[nbm2] * p[nbm2] / p[nden];
+  const R ca3 = p[nbm3] * p[nbm3] / p[nden];
+  const R cts = css + ca1 + ca2 + ca3;
+  const R cm1 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca1)) / R(2));
+  const R ch1 = (fabs(p[nve1]) + cm1);
+  const R cm2 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca2)) / R(2));
+  const R ch2 = (fabs(p[nve2]) + cm2);
+  const R cm3 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca3)) / R(2));
+  const R ch3 = (fabs(p[nve3]) + cm3);
+  R m = ch1;
+  if (m < ch2) m = ch2;
+  if (m < ch3) m = ch3;
+  return m;
+}
+
+}  // namespace MHDGB_VNS
+}  // namespace mhdgb

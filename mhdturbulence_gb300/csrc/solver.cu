@@ -1,0 +1,800 @@
+// solver.cu -- host side of the C ABI declared in include/mhdgb.h.
+//
+// A handle owns, on its device: the conserved state U (FP64), two primitive buffers per precision
+// (the fused step reads one and writes the other), the three face-flux arrays and the pack buffers
+// of the stage path, the per-axis spacing tables, and the control block (Ctrl).  All arrays use
+// the reference FieldArray layout with a padded i pitch; host transfers are 2-D pitched copies.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mhdgb.h"
+#include "kernels.h"
+
+using namespace mhdgb;
+
+// Diagnostic and initial-state kernels (no FP contraction concerns: FP64 sums in fixed order).
+namespace {
+
+template <class R>
+__global__ void k_diag_planes(const R* __restrict__ P, Layout L, const double* __restrict__ dxs,
+                              const double* __restrict__ dys, const double* __restrict__ dzs, double* planes) {
+  // one block per interior k plane; fixed-order tree sum of (dv, X(1-X)dv, vy^2 dv)
+  __shared__ double sh[3][256];
+  const int k = blockIdx.x;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int t = threadIdx.x; t < L.nx * L.ny; t += blockDim.x) {
+    const int i = t % L.nx, j = t / L.nx;
+    const double dv = dxs[i + NGH] * dys[j + NGH] * dzs[k + NGH];
+    const double X = (double)P[L.at(NPRIM, nst, k + NGH, j + NGH, i + NGH)];
+    const double vy = (double)P[L.at(NPRIM, nve2, k + NGH, j + NGH, i + NGH)];
+    s0 += dv;
+    s1 += X * (1.0 - X) * dv;
+    s2 += vy * vy * dv;
+  }
+  sh[0][threadIdx.x] = s0; sh[1][threadIdx.x] = s1; sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int q = 0; q < 3; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; q++) planes[3 * k + q] = sh[q][0];
+}
+
+__global__ void k_diag_final(const double* planes, int nz, double* out) {
+  double v = 0.0, m = 0.0, a = 0.0;
+  for (int k = 0; k < nz; k++) { v += planes[3 * k]; m += planes[3 * k + 1]; a += planes[3 * k + 2]; }
+  out[0] = v;
+  out[1] = m / v;
+  out[2] = sqrt(a / v);
+}
+
+__global__ void k_ctrl_reset(Ctrl* c, int keep_clock) {
+  for (int s = 0; s < 3; s++) { c->slot[s].dtmin_bits = DT_RESET; c->slot[s].chmax_bits = CH_RESET; }
+  if (!keep_clock) { c->step = 0; c->time = 0.0; c->last_dt = 0.0; c->last_ch = 0.0; }
+  c->done = 0;
+  c->status = 0;
+  c->blocks_done = 0;
+  c->work_next = 0;
+}
+
+__global__ void k_ctrl_set_stop(Ctrl* c, double tmax, unsigned long long max_step) {
+  c->tmax = tmax;
+  c->max_step = max_step;
+  c->done = (c->time > tmax || c->step >= max_step) ? 1u : 0u;
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    b[t] = (float)a[t];
+}
+
+uint64_t splitmix64(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+struct mhdgb_solver {
+  mhdgb_config cfg{};
+  FusedKind kind = FUSED_FP64;
+  FusedShape shape{};
+  Layout L{};
+  cudaStream_t stream = nullptr;
+  int nsm = 0;
+  // device memory
+  double* U = nullptr;
+  double* P64[2] = {nullptr, nullptr};
+  float* P32[2] = {nullptr, nullptr};
+  double* F[3] = {nullptr, nullptr, nullptr};
+  double* pack = nullptr;
+  double *xinv = nullptr, *yinv = nullptr, *zinv = nullptr, *dxs = nullptr, *dys = nullptr, *dzs = nullptr;
+  float *xinvf = nullptr, *yinvf = nullptr, *zinvf = nullptr;
+  double* scal = nullptr;   // [0] dt, [1] chg of the stage path, [2..4] diagnostic, [8..] diag planes
+  RedSlot* sslot = nullptr; // stage-path reduction slot
+  Ctrl* ctrl = nullptr;
+  size_t bytes = 0;
+  // host state
+  std::vector<double> x1a, x2a, x3a;
+  CUtensorMap tmap[2];
+  int grid = 0, ntx = 0, nty = 0, nkc = 0, kc = 0;
+  long long cur_step = 0;    // device step count as of the last sync (selects the current P)
+  bool have_state = false;   // U uploaded
+  bool prepared = false;     // fused buffers consistent with U
+  bool p64_valid = false;    // P64[cur] holds the primitives of U (stage path view)
+  cudaGraphExec_t gexec = nullptr;
+  int gsteps = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(mhdgb_solver* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(mhdgb_solver* h, cudaError_t e, const char* what) {
+  return fail(h, MHDGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, call)                                          \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(mhdgb_solver* h, T** p, size_t n) {
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e == cudaSuccess) {
+    h->bytes += n * sizeof(T);
+    e = cudaMemset(*p, 0, n * sizeof(T));
+  }
+  return e;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// 4-D map over a primitive buffer: dims (i, n, j, k) = (itot, 12, jtot, ktot); box (tx+4, 12, ty+4, 1).
+int make_tmap(mhdgb_solver* h, CUtensorMap* map, void* base, int elem) {
+  auto fn = encode_fn();
+  if (!fn) return fail(h, MHDGB_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const Layout& L = h->L;
+  cuuint64_t dims[4] = {(cuuint64_t)L.itot, (cuuint64_t)NPRIM, (cuuint64_t)L.jtot, (cuuint64_t)L.ktot};
+  cuuint64_t strides[3] = {(cuuint64_t)L.ip * elem, (cuuint64_t)L.ip * elem * NPRIM,
+                           (cuuint64_t)L.ip * elem * NPRIM * L.jtot};
+  cuuint32_t box[4] = {(cuuint32_t)(h->shape.tx + 4), (cuuint32_t)NPRIM, (cuuint32_t)(h->shape.ty + 4), 1u};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = fn(map, elem == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(h, MHDGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return MHDGB_OK;
+}
+
+void set_spacing_tables(mhdgb_solver* h, std::vector<double>& hx, std::vector<double>& hinv,
+                        const std::vector<double>& xa, int n) {
+  hx.assign(n, 0.0);
+  hinv.assign(n, 0.0);
+  for (int i = 0; i + 1 < (int)xa.size(); i++) {
+    hx[i] = xa[i + 1] - xa[i];
+    hinv[i] = 1.0 / (xa[i + 1] - xa[i]);
+  }
+}
+
+int upload_grid(mhdgb_solver* h) {
+  const int n = std::max(h->L.itot, std::max(h->L.jtot, h->L.ktot));
+  std::vector<double> dx, ix, dy, iy, dz, iz;
+  set_spacing_tables(h, dx, ix, h->x1a, n);
+  set_spacing_tables(h, dy, iy, h->x2a, n);
+  set_spacing_tables(h, dz, iz, h->x3a, n);
+  std::vector<float> fx(n), fy(n), fz(n);
+  for (int i = 0; i < n; i++) { fx[i] = (float)ix[i]; fy[i] = (float)iy[i]; fz[i] = (float)iz[i]; }
+  const size_t b = n * sizeof(double), bf = n * sizeof(float);
+  CK(h, cudaMemcpy(h->dxs, dx.data(), b, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->dys, dy.data(), b, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->dzs, dz.data(), b, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->xinv, ix.data(), b, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->yinv, iy.data(), b, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->zinv, iz.data(), b, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->xinvf, fx.data(), bf, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->yinvf, fy.data(), bf, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->zinvf, fz.data(), bf, cudaMemcpyHostToDevice));
+  return MHDGB_OK;
+}
+
+// GenerateGrid (main.cpp:35-64) for one rank.
+std::vector<double> face_axis(int n, double lo, double hi) {
+  const int ngh = NGH, is = ngh, ie = is + n - 1;
+  std::vector<double> xa(n + 2 * ngh + 1);
+  const double xminloc = lo + (hi - lo) / 1 * 0;
+  const double xmaxloc = lo + (hi - lo) / 1 * (0 + 1);
+  const double dx = (xmaxloc - xminloc) / double(n);
+  for (int i = is - ngh; i <= ie + ngh + 1; i++) xa[i] = dx * (i - (ngh + 1)) + xminloc;
+  return xa;
+}
+
+int set_device(mhdgb_solver* h) {
+  CK(h, cudaSetDevice(h->cfg.device));
+  return MHDGB_OK;
+}
+
+// 2-D pitched copy of a reference-layout host array (row = itot elements) to/from a device array.
+int copy_h2d(mhdgb_solver* h, void* dst, const void* src, int nv, size_t elem) {
+  const Layout& L = h->L;
+  CK(h, cudaMemcpy2DAsync(dst, L.ip * elem, src, L.itot * elem, L.itot * elem, (size_t)nv * L.jtot * L.ktot,
+                          cudaMemcpyHostToDevice, h->stream));
+  return MHDGB_OK;
+}
+
+int copy_d2h(mhdgb_solver* h, void* dst, const void* src, int nv, size_t elem) {
+  const Layout& L = h->L;
+  CK(h, cudaMemcpy2DAsync(dst, L.itot * elem, src, L.ip * elem, L.itot * elem, (size_t)nv * L.jtot * L.ktot,
+                          cudaMemcpyDeviceToHost, h->stream));
+  return MHDGB_OK;
+}
+
+int read_ctrl(mhdgb_solver* h, Ctrl* c) {
+  CK(h, cudaMemcpyAsync(c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int status_to_code(mhdgb_solver* h, unsigned st) {
+  if (st & ST_TIMEOUT) return fail(h, MHDGB_ERR_TIMEOUT, "a device-side wait gave up (TMA load did not complete)");
+  if (st & ST_NONFINITE) return fail(h, MHDGB_ERR_NONFINITE, "non-finite dt or c_h candidate in the state");
+  if (st & ST_NEGATIVE) return fail(h, MHDGB_ERR_NEGATIVE, "non-positive density or pressure in the state");
+  return MHDGB_OK;
+}
+
+int cur_index(const mhdgb_solver* h) { return (int)(h->cur_step & 1); }
+
+// Make P64[cur] the primitives of U (interior + ghosts), for the stage path and downloads.
+int ensure_p64(mhdgb_solver* h) {
+  if (h->p64_valid) return MHDGB_OK;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
+  double* P = h->P64[cur_index(h)];
+  CK(h, launch_update_prim(h->U, P, h->L, h->cfg.gam, h->stream));
+  CK(h, launch_ghost_fill(P, h->L, h->cfg.bc, h->pack, h->stream));
+  h->p64_valid = true;
+  return MHDGB_OK;
+}
+
+int destroy_graph(mhdgb_solver* h) {
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  h->gexec = nullptr;
+  h->gsteps = 0;
+  return MHDGB_OK;
+}
+
+FusedArgs fused_args(mhdgb_solver* h) {
+  FusedArgs a{};
+  a.U = h->U;
+  if (h->kind == FUSED_MIXED) { a.P[0] = h->P32[0]; a.P[1] = h->P32[1]; }
+  else { a.P[0] = h->P64[0]; a.P[1] = h->P64[1]; }
+  a.L = h->L;
+  a.xinv = h->xinv; a.yinv = h->yinv; a.zinv = h->zinv;
+  a.dxs = h->dxs; a.dys = h->dys; a.dzs = h->dzs;
+  a.xinvf = h->xinvf; a.yinvf = h->yinvf; a.zinvf = h->zinvf;
+  a.gam = h->cfg.gam;
+  a.cfl = h->cfg.cfl;
+  for (int q = 0; q < 6; q++) a.bc[q] = h->cfg.bc[q];
+  a.quirk = h->cfg.spacing_quirk;
+  a.ntx = h->ntx; a.nty = h->nty; a.nkc = h->nkc; a.kc = h->kc;
+  a.ctrl = h->ctrl;
+  return a;
+}
+
+int launch_one(mhdgb_solver* h) {
+  FusedArgs a = fused_args(h);
+  CK(h, launch_fused(h->kind, h->tmap, a, h->grid, h->stream));
+  return MHDGB_OK;
+}
+
+int build_graph(mhdgb_solver* h, int nsteps) {
+  destroy_graph(h);
+  cudaGraph_t g = nullptr;
+  CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = MHDGB_OK;
+  for (int s = 0; s < nsteps && rc == MHDGB_OK; s++) rc = launch_one(h);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (rc != MHDGB_OK) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&h->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+  h->gsteps = nsteps;
+  return MHDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhdgb_config_default(mhdgb_config* c) {
+  if (!c) return MHDGB_ERR_ARG;
+  std::memset(c, 0, sizeof(*c));
+  c->nx = c->ny = c->nz = 150;
+  c->x1min = -0.5; c->x1max = 0.5;
+  c->x2min = -1.0; c->x2max = 1.0;
+  c->x3min = -0.5; c->x3max = 0.5;
+  c->bc[0] = c->bc[1] = MHDGB_BC_PERIODIC;
+  c->bc[2] = c->bc[3] = MHDGB_BC_REFLECTION;
+  c->bc[4] = c->bc[5] = MHDGB_BC_PERIODIC;
+  c->gam = 5.0 / 3.0;
+  c->cfl = 0.05;
+  c->precision = MHDGB_FP64;
+  c->spacing_quirk = 0;
+  c->device = 0;
+  return MHDGB_OK;
+}
+
+const char* mhdgb_status_string(int s) {
+  switch (s) {
+    case MHDGB_OK: return "ok";
+    case MHDGB_ERR_ARG: return "invalid argument";
+    case MHDGB_ERR_CUDA: return "CUDA error";
+    case MHDGB_ERR_NONFINITE: return "non-finite value in the state";
+    case MHDGB_ERR_NEGATIVE: return "non-positive density or pressure";
+    case MHDGB_ERR_TIMEOUT: return "device-side wait timed out";
+    case MHDGB_ERR_STATE: return "call out of order";
+    case MHDGB_ERR_NOMEM: return "device allocation failed";
+    default: return "unknown status";
+  }
+}
+
+const char* mhdgb_last_error(const mhdgb_solver* h) { return h ? h->err.c_str() : "null handle"; }
+
+int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
+  if (!cfg || !out) return MHDGB_ERR_ARG;
+  *out = nullptr;
+  if (cfg->nx < 2 || cfg->ny < 2 || cfg->nz < 2) return MHDGB_ERR_ARG;
+  if (!(cfg->gam > 1.0) || !(cfg->cfl > 0.0)) return MHDGB_ERR_ARG;
+  for (int q = 0; q < 6; q++)
+    if (cfg->bc[q] < 1 || cfg->bc[q] > 3) return MHDGB_ERR_ARG;
+  if (cfg->precision < MHDGB_FP64 || cfg->precision > MHDGB_MIXED) return MHDGB_ERR_ARG;
+  if (cfg->spacing_quirk && (cfg->nx > cfg->ny || cfg->nx > cfg->nz)) return MHDGB_ERR_ARG;
+  mhdgb_solver* h = new mhdgb_solver();
+  h->cfg = *cfg;
+  int rc = set_device(h);
+  if (rc) { delete h; return rc; }
+  h->kind = cfg->precision == MHDGB_MIXED ? FUSED_MIXED : (cfg->precision == MHDGB_FP64_EXACT ? FUSED_FP64_EXACT : FUSED_FP64);
+  h->shape = fused_shape(h->kind);
+  Layout& L = h->L;
+  L.nx = cfg->nx; L.ny = cfg->ny; L.nz = cfg->nz;
+  L.itot = cfg->nx + 2 * NGH + 1; L.jtot = cfg->ny + 2 * NGH + 1; L.ktot = cfg->nz + 2 * NGH + 1;
+  L.ip = (L.itot + 7) / 8 * 8;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, cfg->device) != cudaSuccess) { delete h; return MHDGB_ERR_CUDA; }
+  h->nsm = prop.multiProcessorCount;
+  auto cleanup = [&](int code) { mhdgb_destroy(h); return code; };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
+  const int nmax = std::max(L.itot, std::max(L.jtot, L.ktot));
+  bool ok = dalloc(h, &h->U, L.count(NCONS)) == cudaSuccess;
+  for (int q = 0; q < 2 && ok; q++) ok = dalloc(h, &h->P64[q], L.count(NPRIM)) == cudaSuccess;
+  if (h->kind == FUSED_MIXED)
+    for (int q = 0; q < 2 && ok; q++) ok = dalloc(h, &h->P32[q], L.count(NPRIM)) == cudaSuccess;
+  for (int q = 0; q < 3 && ok; q++) ok = dalloc(h, &h->F[q], L.count(NCONS)) == cudaSuccess;
+  ok = ok && dalloc(h, &h->pack, pack_buffer_doubles(L)) == cudaSuccess;
+  ok = ok && dalloc(h, &h->xinv, nmax) == cudaSuccess && dalloc(h, &h->yinv, nmax) == cudaSuccess &&
+       dalloc(h, &h->zinv, nmax) == cudaSuccess && dalloc(h, &h->dxs, nmax) == cudaSuccess &&
+       dalloc(h, &h->dys, nmax) == cudaSuccess && dalloc(h, &h->dzs, nmax) == cudaSuccess &&
+       dalloc(h, &h->xinvf, nmax) == cudaSuccess && dalloc(h, &h->yinvf, nmax) == cudaSuccess &&
+       dalloc(h, &h->zinvf, nmax) == cudaSuccess;
+  ok = ok && dalloc(h, &h->scal, 8 + 3 * (size_t)L.nz) == cudaSuccess;
+  ok = ok && dalloc(h, &h->sslot, 1) == cudaSuccess && dalloc(h, &h->ctrl, 1) == cudaSuccess;
+  if (!ok) return cleanup(MHDGB_ERR_NOMEM);
+  h->x1a = face_axis(cfg->nx, cfg->x1min, cfg->x1max);
+  h->x2a = face_axis(cfg->ny, cfg->x2min, cfg->x2max);
+  h->x3a = face_axis(cfg->nz, cfg->x3min, cfg->x3max);
+  if ((rc = upload_grid(h))) return cleanup(rc);
+  if (fused_prepare(h->kind) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
+  const int cps = std::max(1, fused_ctas_per_sm(h->kind));
+  h->grid = h->nsm * cps;
+  h->ntx = (L.nx + h->shape.tx - 1) / h->shape.tx;
+  h->nty = (L.ny + h->shape.ty - 1) / h->shape.ty;
+  // z chunks: aim for >= 4 work items per CTA for load balance, chunks of >= 4 planes
+  const int tiles = h->ntx * h->nty;
+  int nkc = (4 * h->grid + tiles - 1) / tiles;
+  nkc = std::max(1, std::min(nkc, L.nz / 4 > 0 ? L.nz / 4 : 1));
+  h->kc = (L.nz + nkc - 1) / nkc;
+  h->nkc = (L.nz + h->kc - 1) / h->kc;
+  void* pbase[2] = {h->kind == FUSED_MIXED ? (void*)h->P32[0] : (void*)h->P64[0],
+                    h->kind == FUSED_MIXED ? (void*)h->P32[1] : (void*)h->P64[1]};
+  for (int q = 0; q < 2; q++)
+    if ((rc = make_tmap(h, &h->tmap[q], pbase[q], h->shape.elem))) return cleanup(rc);
+  k_ctrl_reset<<<1, 1, 0, h->stream>>>(h->ctrl, 0);
+  k_ctrl_set_stop<<<1, 1, 0, h->stream>>>(h->ctrl, 1.0e300, ~0ull);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
+  *out = h;
+  return MHDGB_OK;
+}
+
+int mhdgb_destroy(mhdgb_solver* h) {
+  if (!h) return MHDGB_OK;
+  cudaSetDevice(h->cfg.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  destroy_graph(h);
+  void* ptrs[] = {h->U, h->P64[0], h->P64[1], h->P32[0], h->P32[1], h->F[0], h->F[1], h->F[2], h->pack,
+                  h->xinv, h->yinv, h->zinv, h->dxs, h->dys, h->dzs, h->xinvf, h->yinvf, h->zinvf,
+                  h->scal, h->sslot, h->ctrl};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MHDGB_OK;
+}
+
+int mhdgb_extents(const mhdgb_solver* h, int* itot, int* jtot, int* ktot) {
+  if (!h) return MHDGB_ERR_ARG;
+  if (itot) *itot = h->L.itot;
+  if (jtot) *jtot = h->L.jtot;
+  if (ktot) *ktot = h->L.ktot;
+  return MHDGB_OK;
+}
+
+size_t mhdgb_device_bytes(const mhdgb_solver* h) { return h ? h->bytes : 0; }
+
+int mhdgb_get_grid(const mhdgb_solver* h, double* x1a, double* x2a, double* x3a) {
+  if (!h) return MHDGB_ERR_ARG;
+  if (x1a) std::memcpy(x1a, h->x1a.data(), h->x1a.size() * sizeof(double));
+  if (x2a) std::memcpy(x2a, h->x2a.data(), h->x2a.size() * sizeof(double));
+  if (x3a) std::memcpy(x3a, h->x3a.data(), h->x3a.size() * sizeof(double));
+  return MHDGB_OK;
+}
+
+int mhdgb_set_grid(mhdgb_solver* h, const double* x1a, const double* x2a, const double* x3a) {
+  if (!h || !x1a || !x2a || !x3a) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  h->x1a.assign(x1a, x1a + h->L.itot);
+  h->x2a.assign(x2a, x2a + h->L.jtot);
+  h->x3a.assign(x3a, x3a + h->L.ktot);
+  h->prepared = false;
+  return upload_grid(h);
+}
+
+int mhdgb_upload_cons(mhdgb_solver* h, const double* U) {
+  if (!h || !U) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = copy_h2d(h, h->U, U, NCONS, sizeof(double)))) return rc;
+  h->have_state = true;
+  h->prepared = false;
+  h->p64_valid = false;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_upload_prim(mhdgb_solver* h, const double* P) {
+  if (!h || !P) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = copy_h2d(h, h->P64[cur_index(h)], P, NPRIM, sizeof(double)))) return rc;
+  h->p64_valid = true;
+  h->prepared = false;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_download_cons(mhdgb_solver* h, double* U) {
+  if (!h || !U) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = copy_d2h(h, U, h->U, NCONS, sizeof(double)))) return rc;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_download_prim(mhdgb_solver* h, double* P) {
+  if (!h || !P) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = mhdgb_sync(h, nullptr)) < 0) {
+    if (rc != MHDGB_ERR_NONFINITE && rc != MHDGB_ERR_NEGATIVE) return rc;
+  }
+  if ((rc = ensure_p64(h))) return rc;
+  if ((rc = copy_d2h(h, P, h->P64[cur_index(h)], NPRIM, sizeof(double)))) return rc;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_download_flux(mhdgb_solver* h, int dir, double* F) {
+  if (!h || !F || dir < 1 || dir > 3) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = copy_d2h(h, F, h->F[dir - 1], NCONS, sizeof(double)))) return rc;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+// ---- stage entry points ----
+int mhdgb_control_timestep(mhdgb_solver* h, double* dt) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = ensure_p64(h))) return rc;
+  CK(h, launch_reduce_dt_ch(h->P64[cur_index(h)], h->L, h->dxs, h->dys, h->dzs, h->sslot, &h->ctrl->status, h->nsm,
+                            h->stream));
+  double tmp[2];
+  CK(h, launch_slot_to_scalars(h->sslot, h->cfg.cfl, h->scal + 2, h->scal + 3, h->stream));
+  CK(h, cudaMemcpyAsync(h->scal + 0, h->scal + 2, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(tmp, h->scal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (dt) *dt = tmp[0];
+  return MHDGB_OK;
+}
+
+int mhdgb_set_boundary(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = ensure_p64(h))) return rc;
+  CK(h, launch_ghost_fill(h->P64[cur_index(h)], h->L, h->cfg.bc, h->pack, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_evaluate_ch(mhdgb_solver* h, double* chg) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = ensure_p64(h))) return rc;
+  CK(h, launch_reduce_dt_ch(h->P64[cur_index(h)], h->L, h->dxs, h->dys, h->dzs, h->sslot, &h->ctrl->status, h->nsm,
+                            h->stream));
+  double tmp[2];
+  CK(h, launch_slot_to_scalars(h->sslot, h->cfg.cfl, h->scal + 2, h->scal + 3, h->stream));
+  CK(h, cudaMemcpyAsync(h->scal + 1, h->scal + 3, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(tmp, h->scal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (chg) *chg = tmp[1];
+  return MHDGB_OK;
+}
+
+int mhdgb_flux(mhdgb_solver* h, int dir) {
+  if (!h || dir < 1 || dir > 3) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = ensure_p64(h))) return rc;
+  CK(h, launch_flux(dir, h->P64[cur_index(h)], h->F[dir - 1], h->L, h->scal + 1, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_update_conserv(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
+  CK(h, launch_update_conserv(h->F[0], h->F[1], h->F[2], h->U, h->L, h->xinv, h->yinv, h->zinv,
+                              h->cfg.spacing_quirk, h->scal + 0, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->prepared = false;
+  return MHDGB_OK;
+}
+
+int mhdgb_damp_psi(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
+  CK(h, launch_damp_psi(h->U, h->L, h->dxs, h->dys, h->dzs, h->scal + 0, h->scal + 1, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->prepared = false;
+  return MHDGB_OK;
+}
+
+int mhdgb_update_prim(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
+  CK(h, launch_update_prim(h->U, h->P64[cur_index(h)], h->L, h->cfg.gam, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->p64_valid = true;
+  h->prepared = false;
+  return MHDGB_OK;
+}
+
+int mhdgb_set_dt(mhdgb_solver* h, double dt) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  CK(h, cudaMemcpy(h->scal + 0, &dt, sizeof(double), cudaMemcpyHostToDevice));
+  return MHDGB_OK;
+}
+
+int mhdgb_set_chg(mhdgb_solver* h, double chg) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  CK(h, cudaMemcpy(h->scal + 1, &chg, sizeof(double), cudaMemcpyHostToDevice));
+  return MHDGB_OK;
+}
+
+// ---- fused step ----
+int mhdgb_prepare(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
+  Ctrl c;
+  if ((rc = read_ctrl(h, &c))) return rc;
+  h->cur_step = (long long)c.step;
+  const int cur = cur_index(h);
+  void* P = h->kind == FUSED_MIXED ? (void*)h->P32[cur] : (void*)h->P64[cur];
+  CK(h, launch_reset_slot(&h->ctrl->slot[c.step % 3], h->stream));
+  CK(h, launch_reset_slot(&h->ctrl->slot[(c.step + 1) % 3], h->stream));
+  CK(h, launch_recover(h->kind, h->U, P, h->L, h->cfg.bc, h->dxs, h->dys, h->dzs, h->cfg.gam,
+                       &h->ctrl->slot[c.step % 3], &h->ctrl->status, h->nsm, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->prepared = true;
+  h->p64_valid = h->kind != FUSED_MIXED;
+  return MHDGB_OK;
+}
+
+int mhdgb_step(mhdgb_solver* h, int nsteps) {
+  if (!h || nsteps < 0) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->prepared && (rc = mhdgb_prepare(h))) return rc;
+  const int G = 16;
+  if (nsteps >= G && !h->gexec && (rc = build_graph(h, G))) return rc;
+  while (nsteps >= G) {
+    CK(h, cudaGraphLaunch(h->gexec, h->stream));
+    nsteps -= G;
+  }
+  for (; nsteps > 0; nsteps--)
+    if ((rc = launch_one(h))) return rc;
+  h->p64_valid = false;
+  return MHDGB_OK;
+}
+
+int mhdgb_set_stop(mhdgb_solver* h, double tmax, long long max_steps) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  k_ctrl_set_stop<<<1, 1, 0, h->stream>>>(h->ctrl, tmax, max_steps < 0 ? ~0ull : (unsigned long long)max_steps);
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_sync(mhdgb_solver* h, mhdgb_report* r) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  Ctrl c;
+  if ((rc = read_ctrl(h, &c))) return rc;
+  if ((long long)c.step != h->cur_step) {
+    h->cur_step = (long long)c.step;
+    h->p64_valid = false;
+  }
+  if (r) {
+    r->step = (long long)c.step;
+    r->time = c.time;
+    r->dt = c.last_dt;
+    r->chg = c.last_ch;
+    r->next_dt = h->cfg.cfl * bitsd(c.slot[c.step % 3].dtmin_bits);
+    r->next_chg = bitsd(c.slot[c.step % 3].chmax_bits);
+    r->done = (int)c.done;
+    r->status = c.status;
+  }
+  return status_to_code(h, c.status);
+}
+
+int mhdgb_run_until(mhdgb_solver* h, double tmax, long long max_steps, mhdgb_report* r) {
+  int rc = mhdgb_set_stop(h, tmax, max_steps);
+  if (rc) return rc;
+  mhdgb_report rep;
+  for (;;) {
+    if ((rc = mhdgb_step(h, 64))) return rc;
+    if ((rc = mhdgb_sync(h, &rep))) return rc;
+    if (rep.done) break;
+  }
+  if (r) *r = rep;
+  return MHDGB_OK;
+}
+
+int mhdgb_reset_clock(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  k_ctrl_reset<<<1, 1, 0, h->stream>>>(h->ctrl, 0);
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->cur_step = 0;
+  h->prepared = false;
+  h->p64_valid = false;
+  return MHDGB_OK;
+}
+
+int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nsteps, double* dt, double* chg) {
+  if (!h || !U_in || !U_out || nsteps < 1) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = copy_h2d(h, h->U, U_in, NCONS, sizeof(double)))) return rc;
+  h->have_state = true;
+  h->prepared = false;
+  if ((rc = mhdgb_prepare(h)) || (rc = mhdgb_step(h, nsteps))) return rc;
+  if ((rc = copy_d2h(h, U_out, h->U, NCONS, sizeof(double)))) return rc;
+  mhdgb_report rep;
+  rc = mhdgb_sync(h, &rep);
+  if (dt) *dt = rep.dt;
+  if (chg) *chg = rep.chg;
+  return rc;
+}
+
+int mhdgb_time_steps(mhdgb_solver* h, int nsteps, double* ms) {
+  if (!h || nsteps < 1 || !ms) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->prepared && (rc = mhdgb_prepare(h))) return rc;
+  const int G = 16;
+  if (nsteps >= G && !h->gexec && (rc = build_graph(h, G))) return rc;
+  cudaEvent_t e0, e1;
+  CK(h, cudaEventCreate(&e0));
+  CK(h, cudaEventCreate(&e1));
+  CK(h, cudaStreamSynchronize(h->stream));
+  CK(h, cudaEventRecord(e0, h->stream));
+  rc = mhdgb_step(h, nsteps);
+  CK(h, cudaEventRecord(e1, h->stream));
+  CK(h, cudaEventSynchronize(e1));
+  float t = 0.0f;
+  CK(h, cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t;
+  return rc;
+}
+
+int mhdgb_diag(mhdgb_solver* h, double out[3]) {
+  if (!h || !out) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = mhdgb_sync(h, nullptr)) == MHDGB_ERR_CUDA) return rc;
+  const Layout& L = h->L;
+  double* planes = h->scal + 8;
+  if (h->kind == FUSED_MIXED && h->prepared) {
+    k_diag_planes<float><<<L.nz, 256, 0, h->stream>>>(h->P32[cur_index(h)], L, h->dxs, h->dys, h->dzs, planes);
+  } else {
+    if ((rc = ensure_p64(h))) return rc;
+    k_diag_planes<double><<<L.nz, 256, 0, h->stream>>>(h->P64[cur_index(h)], L, h->dxs, h->dys, h->dzs, planes);
+  }
+  CK(h, cudaGetLastError());
+  k_diag_final<<<1, 1, 0, h->stream>>>(planes, L.nz, h->scal + 4);
+  CK(h, cudaGetLastError());
+  CK(h, cudaMemcpyAsync(out, h->scal + 4, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, double width, double bx, double amp,
+                  double sig, double noise) {
+  if (!h) return MHDGB_ERR_ARG;
+  const Layout& L = h->L;
+  const int it = L.itot, jt = L.jtot;
+  std::vector<double> U((size_t)NCONS * it * jt * L.ktot, 0.0);
+  const double pi = std::acos(-1.0), gam = h->cfg.gam;
+  const uint64_t key = splitmix64((uint64_t)seed * 0xD1B54A32D192ED03ull + 0ull * 0x8CB92BA72F3D8DD7ull);
+  for (int k = 0; k < L.nz; k++)
+    for (int j = 0; j < L.ny; j++)
+      for (int i = 0; i < L.nx; i++) {
+        const double x = 0.5 * (h->x1a[i + NGH + 1] + h->x1a[i + NGH]);
+        const double y = 0.5 * (h->x2a[j + NGH + 1] + h->x2a[j + NGH]);
+        const uint64_t idx = ((uint64_t)k * L.ny + j) * L.nx + i;
+        const double u = (double)(splitmix64(idx ^ key) >> 11) * (1.0 / 9007199254740992.0);
+        const double th = std::tanh(y / width);
+        const double rho = 1.0, p = 1.0;
+        const double vx = vshear * th;
+        const double vy = amp * std::sin(2.0 * pi * x) * std::exp(-(y / sig) * (y / sig)) + noise * (2.0 * u - 1.0);
+        const double vz = 0.0, by = 0.0, bz = 0.0, X = 0.5 * (1.0 + th);
+        const double e = p / (rho * (gam - 1.0));
+        const double ekin = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
+        const double emag = 0.5 * (bx * bx + by * by + bz * bz);
+        auto at = [&](int m) { return (size_t)(i + NGH) + (size_t)it * (m + (size_t)NCONS * ((j + NGH) + (size_t)jt * (k + NGH))); };
+        U[at(mden)] = rho;
+        U[at(mrv1)] = rho * vx;
+        U[at(mrv2)] = rho * vy;
+        U[at(mrv3)] = rho * vz;
+        U[at(meto)] = rho * e + ekin + emag;
+        U[at(mbm1)] = bx;
+        U[at(mbm2)] = by;
+        U[at(mbm3)] = bz;
+        U[at(mbps)] = 0.0;
+        U[at(mst)] = rho * X;
+      }
+  return mhdgb_upload_cons(h, U.data());
+}
+
+}  // extern "C"

@@ -32,13 +32,16 @@ static void dump(FILE* f, const FieldArray<double>& A) {
 }
 
 static void setup_grid(GridArray<double>& G) {
-  // single-rank form of main.cpp:35-64 (coords = 0, ntiles = 1)
-  const double dx1 = (x1max - x1min) / double(ngrid1);
-  for (int i = is - ngh; i <= ie + ngh + 1; i++) G.x1a(i) = dx1 * (i - (ngh + 1)) + x1min;
-  const double dx2 = (x2max - x2min) / double(ngrid2);
-  for (int j = js - ngh; j <= je + ngh + 1; j++) G.x2a(j) = dx2 * (j - (ngh + 1)) + x2min;
-  const double dx3 = (x3max - x3min) / double(ngrid3);
-  for (int k = ks - ngh; k <= ke + ngh + 1; k++) G.x3a(k) = dx3 * (k - (ngh + 1)) + x3min;
+  // single-rank form of main.cpp:35-64 (coords = 0, ntiles = 1), same operations
+  const double x1minloc = x1min + (x1max - x1min) / 1 * 0, x1maxloc = x1min + (x1max - x1min) / 1 * (0 + 1);
+  const double dx1 = (x1maxloc - x1minloc) / double(ngrid1);
+  for (int i = is - ngh; i <= ie + ngh + 1; i++) G.x1a(i) = dx1 * (i - (ngh + 1)) + x1minloc;
+  const double x2minloc = x2min + (x2max - x2min) / 1 * 0, x2maxloc = x2min + (x2max - x2min) / 1 * (0 + 1);
+  const double dx2 = (x2maxloc - x2minloc) / double(ngrid2);
+  for (int j = js - ngh; j <= je + ngh + 1; j++) G.x2a(j) = dx2 * (j - (ngh + 1)) + x2minloc;
+  const double x3minloc = x3min + (x3max - x3min) / 1 * 0, x3maxloc = x3min + (x3max - x3min) / 1 * (0 + 1);
+  const double dx3 = (x3maxloc - x3minloc) / double(ngrid3);
+  for (int k = ks - ngh; k <= ke + ngh + 1; k++) G.x3a(k) = dx3 * (k - (ngh + 1)) + x3minloc;
 }
 
 int main(int argc, char** argv) {

@@ -1,0 +1,238 @@
+"""Parity of the CUDA path with the reference (golden vectors made by the reference's own stages)
+and with the oracle, through the C ABI of libmhdgb.so.
+
+Tolerances (from the benchmark spec of the FP64 form): relative L-infinity <= 1e-12 after one
+step and <= 1e-9 after 100 steps for the FMA-contracted FP64 fused step; bit-for-bit equality
+for the stage entry points and for the separately rounded FP64 fused step."""
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_cases import cases
+from mhdturbulence_gb300 import MhdgbError, Solver, ic
+
+pytestmark = pytest.mark.gpu
+CASES = cases()
+GAM = 5.0 / 3.0
+
+
+def rel_linf(a, b, floor=1e-3):
+    """max over fields of max|a-b| / max(max|b|, floor); arrays (nz, ny, nv, nx)."""
+    err = 0.0
+    for m in range(b.shape[2]):
+        scale = max(np.abs(b[:, :, m, :]).max(), floor)
+        err = max(err, np.abs(a[:, :, m, :] - b[:, :, m, :]).max() / scale)
+    return err
+
+
+def solver_for(case, precision, quirk=True):
+    return Solver(case.nx, case.ny, case.nz, domain=case.domain, bc=case.bc, gam=case.gam,
+                  precision=precision, spacing_quirk=quirk)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+def test_stage_path_bitwise_vs_reference(case):
+    with solver_for(case, "fp64_exact") as s:
+        s.upload_cons(case.U0())
+        s.UpdatePrimitvP()
+        assert np.array_equal(case.view(s.download_prim()), case.z["P0"])
+        dt, chg = s.stage_step()
+        assert dt == case.z["dts"][0] and chg == case.z["chgs"][0]
+        assert np.array_equal(case.view(s.download_prim()), case.z["P1"])
+        assert np.array_equal(case.view(s.download_cons()), case.z["U1"])
+        for n in range(1, case.nsteps):
+            dt, chg = s.stage_step()
+            assert dt == case.z["dts"][n] and chg == case.z["chgs"][n]
+        assert np.array_equal(case.view(s.download_prim()), case.z["PN"])
+        assert np.array_equal(case.view(s.download_cons()), case.z["UN"])
+
+
+def test_stage_fluxes_bitwise_vs_reference():
+    case = next(c for c in CASES if c.full)
+    with solver_for(case, "fp64_exact") as s:
+        s.upload_cons(case.U0())
+        s.UpdatePrimitvP()
+        s.ControlTimestep()
+        s.SetBoundaryCondition()
+        s.EvaluateCh()
+        for d in (1, 2, 3):
+            s.GetNumericalFluxD(d)
+            assert np.array_equal(s.download_flux(d), case.z["F1"][d - 1]), f"flux dir {d}"
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+def test_fused_exact_bitwise_vs_reference(case):
+    with solver_for(case, "fp64_exact") as s:
+        s.upload_cons(case.U0())
+        s.step(1)
+        r = s.sync()
+        assert r.step == 1 and r.dt == case.z["dts"][0] and r.chg == case.z["chgs"][0]
+        assert np.array_equal(ic.interior(s.download_cons()), ic.interior(case.z["U1"]) if case.full else case.z["U1"])
+        s.step(case.nsteps - 1)
+        r = s.sync()
+        assert r.step == case.nsteps
+        UN = case.z["UN"] if not case.full else ic.interior(case.z["UN"])
+        PN = case.z["PN"] if not case.full else ic.interior(case.z["PN"])
+        assert np.array_equal(ic.interior(s.download_cons()), UN)
+        assert np.array_equal(ic.interior(s.download_prim()), PN)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+def test_fused_fp64_within_tolerance_of_reference(case):
+    with solver_for(case, "fp64") as s:
+        s.upload_cons(case.U0())
+        s.step(1)
+        r = s.sync()
+        U1 = case.z["U1"] if not case.full else ic.interior(case.z["U1"])
+        assert rel_linf(ic.interior(s.download_cons()), U1) <= 1e-12
+        assert abs(r.dt / case.z["dts"][0] - 1) <= 1e-12
+        s.step(case.nsteps - 1)
+        s.sync()
+        UN = case.z["UN"] if not case.full else ic.interior(case.z["UN"])
+        assert rel_linf(ic.interior(s.download_cons()), UN) <= 1e-9
+
+
+def _kh_state(nx, ny, nz, seed=1):
+    return ic.prim_to_cons(ic.kh_prim(nx, ny, nz, seed=seed), GAM)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_exact"])
+def test_fused_vs_oracle_kh_100_steps(precision):
+    nx, ny, nz, nsteps = 24, 40, 20, 100
+    axes = ic.grid(nx, ny, nz, ic.KH_DOMAIN)
+    U0 = _kh_state(nx, ny, nz)
+    orc = O.Oracle(nx, ny, nz, *axes, gam=GAM, bc=ic.KH_BC, spacing_quirk=False)
+    Uo = U0.copy()
+    Po = ic.empty_field(nx, ny, nz, 12)
+    orc.update_prim(Uo, Po)
+    _, dts1, _ = orc.run(Uo, Po, 1)
+    U1o = Uo.copy()
+    _, dts, _ = orc.run(Uo, Po, nsteps - 1)
+    with Solver(nx, ny, nz, precision=precision) as s:
+        s.upload_cons(U0)
+        s.step(1)
+        r = s.sync()
+        e1 = rel_linf(ic.interior(s.download_cons()), ic.interior(U1o))
+        s.step(nsteps - 1)
+        r = s.sync()
+        eN = rel_linf(ic.interior(s.download_cons()), ic.interior(Uo))
+        if precision == "fp64_exact":
+            assert e1 == 0.0 and eN == 0.0
+        assert e1 <= 1e-12, e1
+        assert eN <= 1e-9, eN
+        assert abs(r.time / (dts1.sum() + dts.sum()) - 1) <= 1e-9
+        d = s.diag()
+    do = orc.diag(Po)
+    assert np.allclose(d, do, rtol=1e-9, atol=0)
+
+
+def test_mixed_error_vs_fp64():
+    nx, ny, nz, nsteps = 32, 64, 16, 60
+    U0 = _kh_state(nx, ny, nz, seed=3)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with Solver(nx, ny, nz, precision=prec) as s:
+            s.upload_cons(U0)
+            s.step(nsteps)
+            res[prec] = (s.sync(), s.download_cons())
+    Ud, Um = ic.interior(res["fp64"][1]), ic.interior(res["mixed"][1])
+    rho_l1 = np.abs(Um[:, :, 0, :] - Ud[:, :, 0, :]).sum() / np.abs(Ud[:, :, 0, :]).sum()
+    assert rho_l1 <= 1e-5, rho_l1
+    assert rel_linf(Um, Ud) <= 1e-4
+    assert abs(res["mixed"][0].time / res["fp64"][0].time - 1) <= 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_conservation_periodic(precision):
+    n = 16
+    U0 = ic.prim_to_cons(ic.turbulence_prim(n, seed=4), GAM)
+    with Solver(n, n, n, domain=ic.CUBE_DOMAIN, bc=ic.PERIODIC_BC, precision=precision) as s:
+        s.upload_cons(U0)
+        s.step(30)
+        s.sync()
+        U = ic.interior(s.download_cons())
+    U0i = ic.interior(U0)
+    for m in (0, 1, 2, 3, 4, 5, 6, 7, 9):  # all but psi (damped)
+        tot0, tot = U0i[:, :, m, :].sum(), U[:, :, m, :].sum()
+        scale = np.abs(U0i[:, :, m, :]).sum() + 1e-30
+        assert abs(tot - tot0) / scale <= (1e-13 if precision == "fp64" else 1e-9), (m, tot, tot0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_run_is_deterministic(precision):
+    nx, ny, nz = 40, 24, 36
+    U0 = _kh_state(nx, ny, nz, seed=5)
+    out = []
+    for _ in range(2):
+        with Solver(nx, ny, nz, precision=precision) as s:
+            s.upload_cons(U0)
+            s.step(20)
+            s.sync()
+            out.append(s.download_cons())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_fused_graph_and_single_launches_agree():
+    nx, ny, nz = 20, 20, 20
+    U0 = _kh_state(nx, ny, nz, seed=6)
+    out = []
+    for chunks in ([35], [1] * 35):
+        with Solver(nx, ny, nz) as s:
+            s.upload_cons(U0)
+            for c in chunks:
+                s.step(c)
+            r = s.sync()
+            assert r.step == 35
+            out.append(s.download_cons())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_stop_condition_and_run_until():
+    nx, ny, nz = 16, 16, 16
+    with Solver(nx, ny, nz) as s:
+        s.upload_cons(_kh_state(nx, ny, nz))
+        r = s.run_until(1e300, max_steps=37)
+        assert r.step == 37 and r.done
+        s.step(5)  # no-ops after the stop condition
+        assert s.sync().step == 37
+        s.reset_clock()
+        s.upload_cons(_kh_state(nx, ny, nz))
+        r = s.run_until(0.05)
+        assert r.done and r.time > 0.05 and r.time - r.dt <= 0.05
+
+
+def test_step_host_matches_resident_steps():
+    nx, ny, nz = 16, 24, 12
+    U0 = _kh_state(nx, ny, nz, seed=8)
+    with Solver(nx, ny, nz) as s:
+        Uout = np.zeros_like(U0)
+        dt, _ = s.step_host(U0, Uout, 3)
+    with Solver(nx, ny, nz) as s:
+        s.upload_cons(U0)
+        s.step(3)
+        r = s.sync()
+        assert np.array_equal(ic.interior(Uout), ic.interior(s.download_cons()))
+        assert dt == r.dt
+
+
+def test_nonfinite_state_is_reported():
+    # failure detection without a GPU fault: a NaN planted in the host input makes the step's
+    # dt/c_h candidates non-finite; the device status word turns that into an error at sync.
+    nx, ny, nz = 12, 12, 12
+    U0 = _kh_state(nx, ny, nz)
+    ic.interior(U0)[3, 4, 4, 5] = np.nan
+    with Solver(nx, ny, nz) as s:
+        s.upload_cons(U0)
+        with pytest.raises(MhdgbError) as ei:
+            s.step(1)
+            s.sync()
+        assert ei.value.code in (-3, -4)
+
+
+def test_init_kh_matches_python_generator():
+    nx, ny, nz = 16, 32, 8
+    with Solver(nx, ny, nz) as s:
+        s.init_kh(seed=1)
+        U = ic.interior(s.download_cons())
+    Up = ic.interior(_kh_state(nx, ny, nz, seed=1))
+    assert np.allclose(U, Up, rtol=1e-14, atol=1e-15)
