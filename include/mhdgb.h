@@ -147,6 +147,17 @@ int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nste
  * launches (synchronising before and after); *ms receives the elapsed device time. */
 int mhdgb_time_steps(mhdgb_solver* h, int nsteps, double* ms);
 
+/* Tile shapes of the fused kernel compiled for the handle's precision (the autotuner's choices):
+ * columns tx x ty per tile, threads per CTA; current = 1 for the one in use. */
+int mhdgb_variant_count(const mhdgb_solver* h);
+int mhdgb_variant_info(const mhdgb_solver* h, int idx, int* tx, int* ty, int* threads, int* current);
+int mhdgb_select_variant(mhdgb_solver* h, int idx);
+/* Time every compiled tile shape on the handle's grid (steps fused steps each, from the current
+ * state, which is restored afterwards) and keep the fastest.  The choice is remembered per
+ * (precision, nx, ny, nz) for later handles in the process and, if the environment variable
+ * MHDGB_TUNE_CACHE names a file, across processes. */
+int mhdgb_autotune(mhdgb_solver* h, int steps, int* best);
+
 /* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):
  * out = {volume, <X(1-X)>, sqrt(<v_y^2>)} over the interior, FP64 sums. */
 int mhdgb_diag(mhdgb_solver* h, double out[3]);

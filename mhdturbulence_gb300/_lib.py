@@ -66,6 +66,11 @@ SIGNATURES = {
     "mhdgb_reset_clock": (C.c_int, [_vp]),
     "mhdgb_step_host": (C.c_int, [_vp, _dp, _dp, C.c_int, _dp, _dp]),
     "mhdgb_time_steps": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_variant_count": (C.c_int, [_vp]),
+    "mhdgb_variant_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]),
+    "mhdgb_select_variant": (C.c_int, [_vp, C.c_int]),
+    "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mhdgb_diag": (C.c_int, [_vp, _dp]),
     "mhdgb_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double]),

@@ -4,7 +4,8 @@
 
 Translation units are compiled in parallel with nvcc:
   csrc/stages.cu  -fmad=false   stage kernels + the bit-exact FP64 fused step
-  csrc/fast.cu                  FP64 (FMA-contracted) and FP32-mixed fused steps
+  csrc/fp64.cu                  FP64 fused steps (FMA contraction), several tile shapes
+  csrc/mixed.cu                 FP32-mixed fused steps (fast FP32 div/sqrt), several tile shapes
   csrc/solver.cu                host side of the C ABI (include/mhdgb.h)
 and linked into mhdturbulence_gb300/_build/libmhdgb.so (static CUDA runtime).
 """
@@ -29,7 +30,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I" + os.path.join(ROOT, "include")]
 UNITS = [
     ("stages.cu", ["-fmad=false"]),
-    ("fast.cu", []),
+    ("fp64.cu", []),
+    ("mixed.cu", ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("solver.cu", []),
 ]
 

@@ -70,6 +70,34 @@ constexpr unsigned long long DT_RESET = 0x7FEFFFFFFFFFFFFFull;  // DBL_MAX
 constexpr unsigned long long CH_RESET = 0x0ull;                 // +0.0
 
 // ---------------------------------------------------------------------------------------------
+// FP32 <-> FP64 conversions on the integer pipe.  On GB300 the F2F conversion instructions issue
+// on the FP64 pipe (about 2 per clock per SM), which the mixed form cannot afford per cell; these
+// bit manipulations give the same values for the numbers the solver produces.
+//   f2d_exact: exact widening of a finite float (zero and denormals become a signed zero).
+//   d2f_rne:   narrowing with round-to-nearest-even; magnitudes below the smallest normal float
+//              flush to a signed zero, magnitudes beyond the float range (and inf/NaN) become inf.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned s = u & 0x80000000u, em = u & 0x7FFFFFFFu;
+  unsigned hi = s | ((em >> 3) + (896u << 20));
+  unsigned lo = em << 29;
+  if (em < 0x00800000u) { hi = s; lo = 0u; }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float d2f_rne(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned s = hi & 0x80000000u, ahi = hi & 0x7FFFFFFFu;
+  unsigned r = ((ahi - (896u << 20)) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1FFFFFFFu;
+  r += (unsigned)(rem > 0x10000000u) | ((unsigned)(rem == 0x10000000u) & r);
+  if (ahi < (897u << 20)) r = 0u;
+  if (ahi >= (1151u << 20)) r = 0x7F800000u;
+  return __uint_as_float(s | r);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Block reductions of (min dt, max ch) with a non-finite check, then one atomic per CTA.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ void warp_minmax(double& mn, double& mx) {

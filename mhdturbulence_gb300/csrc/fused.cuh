@@ -1,28 +1,31 @@
 // fused.cuh -- the fused solver step: one persistent launch per time step.
 //
 // Work decomposition.  The interior is cut into column tiles of TX x TY cells, each split along z
-// into chunks of KC planes; a (tile, chunk) pair is one work item and CTAs pull items from a
-// queue in the control block.  A CTA marches through its chunk plane by plane:
+// into chunks of kc planes; a (tile, chunk) pair is one work item and CTAs pull items from a queue
+// in the control block.  A CTA marches through its chunk plane by plane:
 //   * a 4-slot shared-memory ring receives planes of P (12 primitives, the tile plus 2 halo cells
 //     in x and y) through 4-D TMA tensor loads completing on per-slot mbarriers; plane k+4 is
 //     requested when plane k is retired, so each load has a whole plane of compute to land;
-//   * x pass: limited slopes of all 12 primitives (once per cell, van Leer) into shared memory,
-//     then every x face of the plane (prim->cons, HLLD, GLM) into shared memory, then each cell
-//     thread accumulates (F(i+1/2) - F(i-1/2)) * xinv;  y pass likewise;
-//   * z pass: each cell thread owns its column, keeps the z slope and the lower z-face flux in
-//     registers, computes the upper face from ring planes k..k+2, completes the update
-//     U -= dt*(dFx*xinv + dFy*yinv + dFz*zinv) (the reference's rounding order, mhd.cpp:1438-1440),
-//     damps psi (mhd.cpp:1630), recovers P (mhd.cpp:1483-1506) into the other P buffer together
-//     with its ghost images for the next step, and folds the next step's dt / c_h candidates
-//     into a block reduction (mhd.cpp:1542-1550, 1589-1601).
+//   * phase A: every limited slope the plane needs (van Leer, once per cell and direction): x and y
+//     slopes of plane k and the z slope of plane k+1, one work list;
+//   * phase B: every face flux of the plane (prim->cons, HLLD, GLM): x and y faces of plane k and
+//     the z face k+1/2, one work list;
+//   * phase C: each cell thread completes U -= dt*(dFx*xinv + dFy*yinv + dFz*zinv) (the
+//     reference's rounding order, mhd.cpp:1438-1440), damps psi (mhd.cpp:1630), recovers P
+//     (mhd.cpp:1483-1506) into the other P buffer together with the ghost images the next step
+//     needs, and folds the next step's dt / c_h candidates (mhd.cpp:1542-1550, 1589-1601) into a
+//     block reduction; the lower z-face flux of its column stays in registers.
+// Work lists are padded per sub-list to whole warps so that no warp mixes two code paths.
 // Step n reads dt and c_h from ctrl->slot[n%3] (made by step n-1 or by the initial reduction),
 // reduces into slot[(n+1)%3] and resets slot[(n+2)%3]; the last CTA to finish advances the step
-// counter and the simulated time.  All launches of a run are therefore identical and can be
-// captured once in a CUDA graph.
+// counter and the simulated time.  All launches of a run are identical and can be captured once in
+// a CUDA graph.
 //
-// R is the arithmetic type of reconstruction, Riemann solve and the P buffers (double for the
-// FP64 form, float for the mixed form).  The conserved state U, the update, the psi damping and the
-// pressure recovery are FP64 in both forms.
+// R is the arithmetic type of reconstruction, Riemann solve and the P buffers: double for the FP64
+// form, float for the mixed form.  The conserved state U and its update are FP64 in both forms; in
+// the mixed form the flux-divergence terms are summed with compensation (TwoProd/TwoSum in FP32) and
+// the pressure recovery e = (E - m^2/(2 rho) - B^2/2)/rho is FP64 (with 1/rho from an FP32 seed and
+// one FP64 Newton step).
 #pragma once
 
 #include "common.cuh"
@@ -31,19 +34,49 @@
 
 namespace mhdgb {
 
+template <class R, int TX, int TY, int NT>
+struct FusedSmem {
+  static constexpr int NBUF = 4;
+  static constexpr int PX = TX + 4, PY = TY + 4;
+  static constexpr int PLANE = PX * NPRIM * PY;             // elements of one ring plane
+  static constexpr int NSLX = NPRIM * TY * (TX + 2);        // x slopes, cells i in [-1, TX]
+  static constexpr int NSLY = NPRIM * (TY + 2) * TX;        // y slopes, cells j in [-1, TY]
+  static constexpr int NSLZ = NPRIM * TY * TX;              // z slopes of one plane
+  static constexpr int NFX = NCONS * TY * (TX + 1);         // x faces i in [0, TX]
+  static constexpr int NFY = NCONS * (TY + 1) * TX;         // y faces j in [0, TY]
+  static constexpr int NFZ = NCONS * TY * TX;               // z faces k+1/2
+  static constexpr size_t a16(size_t x) { return (x + 15) / 16 * 16; }
+  static constexpr size_t ring_off = 0;
+  static constexpr size_t slx_off = ((size_t)NBUF * PLANE * sizeof(R) + 127) / 128 * 128;
+  static constexpr size_t sly_off = slx_off + a16(NSLX * sizeof(R));
+  static constexpr size_t slz_off = sly_off + a16(NSLY * sizeof(R));
+  static constexpr size_t fx_off = slz_off + a16(2 * NSLZ * sizeof(R));
+  static constexpr size_t fy_off = fx_off + a16(NFX * sizeof(R));
+  static constexpr size_t fz_off = fy_off + a16(NFY * sizeof(R));
+  static constexpr size_t red_off = fz_off + a16(NFZ * sizeof(R));
+  static constexpr size_t bar_off = red_off + 64 * sizeof(double);
+  static constexpr size_t misc_off = bar_off + NBUF * sizeof(uint64_t);  // work item, abort flag
+  static constexpr size_t used = misc_off + 16;
+  static constexpr size_t total = used + 128;  // room to align the base to 128 bytes
+  static constexpr unsigned plane_tx_bytes = (unsigned)(PLANE * sizeof(R));
+  static_assert(NT % 32 == 0 && NT >= TX * TY, "one owner thread per column, whole warps");
+  static_assert((TX * sizeof(R)) % 16 == 0, "TMA x offsets must be 16-byte multiples");
+  static_assert(((TX + 4) * sizeof(R)) % 16 == 0, "TMA box rows must be 16-byte multiples");
+  static_assert(total <= 227 * 1024, "shared memory budget");
+};
+
 namespace MHDGB_VNS {
 
 // Accumulator of the flux divergence dFx*xinv + dFy*yinv + dFz*zinv of one cell.
 // FP64 form: plain FP64 sums in the reference's order.  Mixed form: each FP32 product is split
 // exactly into value + rounding error (TwoProd with an FMA) and the three terms are added with
-// TwoSum, so the pair (hi, lo) carries the sum with compensated rounding; it is rounded to FP64
-// once, for the FP64 state update.  __fmul_rn/__fadd_rn keep the compiler from fusing the steps.
+// TwoSum, so the pair (hi, lo) carries the sum with compensated rounding.  __fmul_rn/__fadd_rn keep
+// the compiler from fusing the steps.
 template <class R> struct DivAcc;
 template <> struct DivAcc<double> {
   double s[NCONS];
   __device__ __forceinline__ void first(int m, double df, double inv) { s[m] = df * inv; }
   __device__ __forceinline__ void add(int m, double df, double inv) { s[m] = s[m] + df * inv; }
-  __device__ __forceinline__ double total(int m) const { return s[m]; }
 };
 template <> struct DivAcc<float> {
   float hi[NCONS], lo[NCONS];
@@ -61,12 +94,23 @@ template <> struct DivAcc<float> {
     hi[m] = s;
     lo[m] = __fadd_rn(lo[m], __fadd_rn(err, e));
   }
-  __device__ __forceinline__ double total(int m) const { return (double)hi[m] + (double)lo[m]; }
+  __device__ __forceinline__ float total(int m) const { return __fadd_rn(hi[m], lo[m]); }
 };
 
-template <class R> __device__ __forceinline__ R inv_of(const double* d, const float* f, int i);
-template <> __device__ __forceinline__ double inv_of<double>(const double* d, const float*, int i) { return d[i]; }
-template <> __device__ __forceinline__ float inv_of<float>(const double*, const float* f, int i) { return f[i]; }
+template <class R> __device__ __forceinline__ R inv_of(const FusedArgs& a, int d, int i);
+template <> __device__ __forceinline__ double inv_of<double>(const FusedArgs& a, int d, int i) {
+  return d == 0 ? a.xinv[i] : (d == 1 ? a.yinv[i] : a.zinv[i]);
+}
+template <> __device__ __forceinline__ float inv_of<float>(const FusedArgs& a, int d, int i) {
+  return d == 0 ? a.xinvf[i] : (d == 1 ? a.yinvf[i] : a.zinvf[i]);
+}
+template <class R> __device__ __forceinline__ R spacing_of(const FusedArgs& a, int d, int i);
+template <> __device__ __forceinline__ double spacing_of<double>(const FusedArgs& a, int d, int i) {
+  return d == 0 ? a.dxs[i] : (d == 1 ? a.dys[i] : a.dzs[i]);
+}
+template <> __device__ __forceinline__ float spacing_of<float>(const FusedArgs& a, int d, int i) {
+  return d == 0 ? a.dxsf[i] : (d == 1 ? a.dysf[i] : a.dzsf[i]);
+}
 
 // Ghost images of a freshly recovered interior cell: the values the reference's ghost fill
 // (boundary.cpp:152-169 and equivalents) would copy from it at the start of the next step.
@@ -83,21 +127,18 @@ __device__ __forceinline__ void write_ghost_images(R* __restrict__ Pout, const L
       Pout[L.at(NPRIM, n, gk + NGH, gj + NGH, gi + NGH)] = v;
     }
   };
-  // x faces
   if (bc[0] == 1) { if (ii >= nx - 2) put(ii - nx, jj, kk, -1); }
   else if (bc[0] == 2) { if (ii <= 1) put(-1 - ii, jj, kk, nve1); }
   else if (bc[0] == 3) { if (ii == 0) { put(-1, jj, kk, -1); put(-2, jj, kk, -1); } }
   if (bc[1] == 1) { if (ii <= 1) put(nx + ii, jj, kk, -1); }
   else if (bc[1] == 2) { if (ii >= nx - 2) put(2 * nx - 1 - ii, jj, kk, nve1); }
   else if (bc[1] == 3) { if (ii == nx - 1) { put(nx, jj, kk, -1); put(nx + 1, jj, kk, -1); } }
-  // y faces
   if (bc[2] == 1) { if (jj >= ny - 2) put(ii, jj - ny, kk, -1); }
   else if (bc[2] == 2) { if (jj <= 1) put(ii, -1 - jj, kk, nve2); }
   else if (bc[2] == 3) { if (jj == 0) { put(ii, -1, kk, -1); put(ii, -2, kk, -1); } }
   if (bc[3] == 1) { if (jj <= 1) put(ii, ny + jj, kk, -1); }
   else if (bc[3] == 2) { if (jj >= ny - 2) put(ii, 2 * ny - 1 - jj, kk, nve2); }
   else if (bc[3] == 3) { if (jj == ny - 1) { put(ii, ny, kk, -1); put(ii, ny + 1, kk, -1); } }
-  // z faces
   if (bc[4] == 1) { if (kk >= nz - 2) put(ii, jj, kk - nz, -1); }
   else if (bc[4] == 2) { if (kk <= 1) put(ii, jj, -1 - kk, nve3); }
   else if (bc[4] == 3) { if (kk == 0) { put(ii, jj, -1, -1); put(ii, jj, -2, -1); } }
@@ -106,38 +147,114 @@ __device__ __forceinline__ void write_ghost_images(R* __restrict__ Pout, const L
   else if (bc[5] == 3) { if (kk == nz - 1) { put(ii, jj, nz, -1); put(ii, jj, nz + 1, -1); } }
 }
 
-// Recover P (type R) and its ghost images from U for one interior cell, and return the cell's dt
-// and c_h candidates.  FP64 arithmetic for the recovery (the pressure e = (E - ekin - emag)/rho);
-// the candidates are evaluated in R.
+// Primitive recovery of one interior cell from its updated conserved state, written with its
+// ghost images, plus the cell's dt and c_h candidates (in R) and the status checks.
 template <class R>
 __device__ __forceinline__ void recover_cell(const double (&u)[NCONS], double gam, R* __restrict__ Pout,
                                              const Layout& L, const int bc[6], int ii, int jj, int kk,
-                                             double dx, double dy, double dz, double& dtc, double& chc,
-                                             unsigned& bad) {
-  double pd[NPRIM];
-  cons2prim<double>(u, gam, pd);
-  R pr[NPRIM];
+                                             R dx, R dy, R dz, R& dtc, R& chc, unsigned& bad);
+
+// FP64 form: UpdatePrimitvP (mhd.cpp:1483-1506) and the reference candidates.
+template <>
+__device__ __forceinline__ void recover_cell<double>(const double (&u)[NCONS], double gam, double* __restrict__ Pout,
+                                                     const Layout& L, const int bc[6], int ii, int jj, int kk,
+                                                     double dx, double dy, double dz, double& dtc, double& chc,
+                                                     unsigned& bad) {
+  double p[NPRIM];
+  cons2prim<double>(u, gam, p);
 #pragma unroll
-  for (int n = 0; n < NPRIM; n++) pr[n] = (R)pd[n];
-#pragma unroll
-  for (int n = 0; n < NPRIM; n++) Pout[L.at(NPRIM, n, kk + NGH, jj + NGH, ii + NGH)] = pr[n];
-  write_ghost_images<R>(Pout, L, bc, ii, jj, kk, pr);
-  dtc = (double)cell_dt<R>(pr, (R)dx, (R)dy, (R)dz);
-  chc = (double)cell_ch<R>(pr);
+  for (int n = 0; n < NPRIM; n++) Pout[L.at(NPRIM, n, kk + NGH, jj + NGH, ii + NGH)] = p[n];
+  write_ghost_images<double>(Pout, L, bc, ii, jj, kk, p);
+  dtc = cell_dt<double>(p, dx, dy, dz);
+  chc = cell_ch<double>(p);
   if (!(dtc == dtc) || !(chc == chc) || isinf(chc)) bad |= ST_NONFINITE;
-  if (!(pd[nden] > 0.0) || !(pd[npre] > 0.0)) bad |= ST_NEGATIVE;
+  if (!(p[nden] > 0.0) || !(p[npre] > 0.0)) bad |= ST_NEGATIVE;
 }
 
-template <class R, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY, 1)
+// Mixed form: the specific internal energy e = (E - m^2/(2 rho) - B^2/2)/rho is computed in FP64
+// (1/rho from an FP32 reciprocal refined by one FP64 Newton step, ~46 bits); the other primitives,
+// which involve no cancellation, are formed in FP32 from the FP32-rounded conserved values;
+// p = e*rho*(gam-1) and c_s = sqrt(e*gam*(gam-1)) as in mhd.cpp:1497-1499.
+template <>
+__device__ __forceinline__ void recover_cell<float>(const double (&u)[NCONS], double gam, float* __restrict__ Pout,
+                                                    const Layout& L, const int bc[6], int ii, int jj, int kk,
+                                                    float dx, float dy, float dz, float& dtc, float& chc,
+                                                    unsigned& bad) {
+  const float rho_f = d2f_rne(u[mden]);
+  const float rinv_f = 1.0f / rho_f;
+  const double r0 = f2d_exact(rinv_f);
+  const double r = fma(r0, fma(-u[mden], r0, 1.0), r0);
+  double m2 = u[mrv1] * u[mrv1];
+  m2 = fma(u[mrv2], u[mrv2], m2);
+  m2 = fma(u[mrv3], u[mrv3], m2);
+  double b2 = u[mbm1] * u[mbm1];
+  b2 = fma(u[mbm2], u[mbm2], b2);
+  b2 = fma(u[mbm3], u[mbm3], b2);
+  double t = fma(-m2, 0.5 * r, u[meto]);
+  t = fma(-0.5, b2, t);
+  const double e = t * r;
+  const float gf = d2f_rne(gam);
+  float p[NPRIM];
+  p[nden] = rho_f;
+  p[nve1] = d2f_rne(u[mrv1]) * rinv_f;
+  p[nve2] = d2f_rne(u[mrv2]) * rinv_f;
+  p[nve3] = d2f_rne(u[mrv3]) * rinv_f;
+  p[nene] = d2f_rne(e);
+  p[npre] = p[nene] * p[nden] * (gf - 1.0f);
+  p[ncsp] = sqrtf(p[nene] * gf * (gf - 1.0f));
+  p[nbm1] = d2f_rne(u[mbm1]);
+  p[nbm2] = d2f_rne(u[mbm2]);
+  p[nbm3] = d2f_rne(u[mbm3]);
+  p[nbps] = d2f_rne(u[mbps]);
+  p[nst] = d2f_rne(u[mst]) * rinv_f;
+#pragma unroll
+  for (int n = 0; n < NPRIM; n++) Pout[L.at(NPRIM, n, kk + NGH, jj + NGH, ii + NGH)] = p[n];
+  write_ghost_images<float>(Pout, L, bc, ii, jj, kk, p);
+  dtc = cell_dt<float>(p, dx, dy, dz);
+  chc = cell_ch<float>(p);
+  if (!(dtc == dtc) || !(chc == chc) || isinf(chc) || isinf(p[nene])) bad |= ST_NONFINITE;
+  if (!(p[nden] > 0.0f) || !(p[npre] > 0.0f)) bad |= ST_NEGATIVE;
+}
+
+// U update of one cell from its summed flux divergence, then psi damping.
+// FP64 form: U - dt*sum (mhd.cpp:1438-1440) and psi*(1 - dt*(0.1*c_h/min(dx,dy,dz))) (mhd.cpp:1628-1630).
+// Mixed form: fma(-dt, sum, U) in FP64 with the compensated FP32 sum widened exactly; the damping
+// factor is formed in FP32 with 1/min(dx,dy,dz) = max of the inverse spacings, applied in FP64.
+__device__ __forceinline__ void update_cell(const DivAcc<double>& acc, const double* __restrict__ Uc, size_t fs,
+                                            double dt, double chd, float, float, const FusedArgs& a, int i, int j,
+                                            int k, double (&u)[NCONS]) {
+#pragma unroll
+  for (int m = 0; m < NCONS; m++) u[m] = Uc[m * fs] - dt * acc.s[m];
+  double dhl = a.dxs[i];
+  if (a.dys[j] < dhl) dhl = a.dys[j];
+  if (a.dzs[k] < dhl) dhl = a.dzs[k];
+  const double taui = 0.1 * chd / dhl;
+  u[mbps] = u[mbps] * (1.0 - dt * taui);
+}
+
+__device__ __forceinline__ void update_cell(const DivAcc<float>& acc, const double* __restrict__ Uc, size_t fs,
+                                            double dt, double, float dtf, float chf, const FusedArgs& a, int i, int j,
+                                            int k, double (&u)[NCONS]) {
+#pragma unroll
+  for (int m = 0; m < NCONS; m++) u[m] = fma(-dt, f2d_exact(acc.total(m)), Uc[m * fs]);
+  const float imax = fmaxf(fmaxf(a.xinvf[i], a.yinvf[j]), a.zinvf[k]);
+  u[mbps] = u[mbps] * f2d_exact(1.0f - dtf * (0.1f * chf * imax));
+}
+
+template <class R, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT, 1)
 k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ CUtensorMap tmap1, FusedArgs a) {
-  using S = FusedSmem<R, TX, TY>;
-  constexpr int NBUF = S::NBUF, PX = S::PX, SX = S::SX, FX = S::FX, NT = TX * TY;
+  using S = FusedSmem<R, TX, TY, NT>;
+  constexpr int NBUF = S::NBUF, PX = S::PX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations
   R* ring = reinterpret_cast<R*>(smem + S::ring_off);
-  R* slp = reinterpret_cast<R*>(smem + S::slope_off);
-  R* flx = reinterpret_cast<R*>(smem + S::flux_off);
+  R* slx = reinterpret_cast<R*>(smem + S::slx_off);
+  R* sly = reinterpret_cast<R*>(smem + S::sly_off);
+  R* slz = reinterpret_cast<R*>(smem + S::slz_off);
+  R* fxs = reinterpret_cast<R*>(smem + S::fx_off);
+  R* fys = reinterpret_cast<R*>(smem + S::fy_off);
+  R* fzs = reinterpret_cast<R*>(smem + S::fz_off);
   double* red = reinterpret_cast<double*>(smem + S::red_off);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::bar_off);
   int& s_item = *reinterpret_cast<int*>(smem + S::misc_off);
@@ -149,14 +266,13 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
   const int tid = threadIdx.x;
   const unsigned long long step = ctrl->step;
   const int par = (int)(step & 1);
-  const R* __restrict__ Pin = reinterpret_cast<const R*>(a.P[par]);
   R* __restrict__ Pout = reinterpret_cast<R*>(a.P[par ^ 1]);
   const CUtensorMap* tmap = par ? &tmap1 : &tmap0;
-  (void)Pin;
-  const RedSlot cur = ctrl->slot[step % 3];
-  const double dt = a.cfl * bitsd(cur.dtmin_bits);
-  const double chd = bitsd(cur.chmax_bits);
+  const RedSlot cur_slot = ctrl->slot[step % 3];
+  const double dt = a.cfl * bitsd(cur_slot.dtmin_bits);
+  const double chd = bitsd(cur_slot.chmax_bits);
   const R chg = (R)chd;
+  const float dtf = (float)dt, chf = (float)chd;
   RedSlot* next = &ctrl->slot[(step + 1) % 3];
   if (blockIdx.x == 0 && tid == 0) {
     ctrl->slot[(step + 2) % 3].dtmin_bits = DT_RESET;
@@ -174,10 +290,11 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
 #pragma unroll
   for (int s = 0; s < NBUF; s++) fills[s] = 0;
 
-  const int tx = tid % TX, ty = tid / TX;
-  double dmin = 1.0e308, cmax = 0.0;
+  const int oi = tid % TX, oj = tid / TX;  // owner column of this thread (if oj < TY)
+  R cmin = R(1e30), cmax = R(0);
   unsigned bad = 0;
   const int nitems = a.ntx * a.nty * a.nkc;
+  const size_t fsU = (size_t)L.ip;  // field stride of U in the (k, j, n, i) layout
 
   for (;;) {
     if (tid == 0) s_item = (int)atomicAdd(&ctrl->work_next, 1u);
@@ -188,12 +305,11 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
     const int i0 = bxi * TX, j0 = byi * TY;
     const int kb = bki * a.kc, ke = min(kb + a.kc, L.nz);
     const int cx = min(TX, L.nx - i0), cy = min(TY, L.ny - j0);
-    const bool own = tx < cx && ty < cy;
-    const int ii = i0 + tx, jj = j0 + ty;
+    const bool own = oj < TY && oi < cx && oj < cy;
+    const int ii = i0 + oi, jj = j0 + oj;
 
-    // ring slot of plane p (p relative to kb-2)
     auto slot_of = [&](int p) { return (p - (kb - 2)) % NBUF; };
-    auto plane = [&](int p) -> R* { return ring + (size_t)slot_of(p) * S::PLANE; };
+    auto plane = [&](int p) -> const R* { return ring + (size_t)slot_of(p) * S::PLANE; };
     auto issue = [&](int p) {  // thread 0 only
       const int s = slot_of(p);
       mbar_arrive_expect_tx(&bars[s], S::plane_tx_bytes);
@@ -203,33 +319,38 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
       const int s = slot_of(p);
       if (!mbar_wait(&bars[s], (fills[s] - 1) & 1, &ctrl->status)) s_abort = 1;
     };
-    // P value of field n at local (i,j) of plane buffer pl; i,j in [-2, T+2)
     auto PV = [&](const R* pl, int n, int i, int j) -> R { return pl[((j + 2) * NPRIM + n) * PX + (i + 2)]; };
+    auto SLX = [&](int n, int i, int j) -> R& { return slx[(n * TY + j) * (TX + 2) + (i + 1)]; };
+    auto SLY = [&](int n, int i, int j) -> R& { return sly[(n * (TY + 2) + (j + 1)) * TX + i]; };
+    auto SLZ = [&](int b, int n, int i, int j) -> R& { return slz[((b * NPRIM + n) * TY + j) * TX + i]; };
+    auto FXS = [&](int m, int i, int j) -> R& { return fxs[(m * TY + j) * (TX + 1) + i]; };
+    auto FYS = [&](int m, int i, int j) -> R& { return fys[(m * (TY + 1) + j) * TX + i]; };
+    auto FZS = [&](int m, int i, int j) -> R& { return fzs[(m * TY + j) * TX + i]; };
 
-    // prologue: planes kb-2 .. kb+1
+    // prologue: planes kb-2 .. kb+1 (ke >= kb+1 so all exist)
     if (tid == 0) {
       fence_proxy_async();
-      for (int p = kb - 2; p < kb - 2 + NBUF; p++)
-        if (p <= ke + 1) issue(p);
+      for (int p = kb - 2; p < kb + 2; p++) issue(p);
     }
 #pragma unroll
-    for (int s = 0; s < NBUF; s++) fills[s]++;  // every slot received one load (all p <= ke+1 here)
-    for (int p = kb - 2; p <= kb + 1; p++) wait_plane(p);
+    for (int s = 0; s < NBUF; s++) fills[s]++;
+    for (int p = kb - 2; p < kb + 2; p++) wait_plane(p);
     __syncthreads();
     if (s_abort) break;
 
-    R zs_cur[NPRIM];   // z slope of the thread's cell at plane k
-    R fz_lo[NCONS];    // flux through face k-1/2
+    R fz_lo[NCONS];  // flux through face k-1/2 of the owner's column
+    int zb = 0;      // slz buffer holding the z slope of the current plane
     if (own) {
       const R *pm2 = plane(kb - 2), *pm1 = plane(kb - 1), *p0 = plane(kb), *pp1 = plane(kb + 1);
       R pl[NPRIM], pr[NPRIM];
 #pragma unroll
       for (int n = 0; n < NPRIM; n++) {
-        const R a2 = PV(pm2, n, tx, ty), a1 = PV(pm1, n, tx, ty), b0 = PV(p0, n, tx, ty), b1 = PV(pp1, n, tx, ty);
+        const R a2 = PV(pm2, n, oi, oj), a1 = PV(pm1, n, oi, oj), b0 = PV(p0, n, oi, oj), b1 = PV(pp1, n, oi, oj);
         const R zsm1 = van_leer(b0 - a1, a1 - a2);
-        zs_cur[n] = van_leer(b1 - b0, b0 - a1);
+        const R zs0 = van_leer(b1 - b0, b0 - a1);
+        SLZ(0, n, oi, oj) = zs0;
         pl[n] = left_state(a1, zsm1);
-        pr[n] = right_state(b0, zs_cur[n]);
+        pr[n] = right_state(b0, zs0);
       }
       face_flux<R, 3>(pl, pr, chg, fz_lo);
     }
@@ -242,117 +363,121 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
     if (kb + 2 <= ke + 1) fills[slot_of(kb + 2)]++;
     if (kb + 3 <= ke + 1) fills[slot_of(kb + 3)]++;
 
+    // work-list sizes (padded to whole warps per sub-list)
+    const int nxs = cy * (cx + 2), nys = (cy + 2) * cx, nzs = cy * cx;
+    const int nxf = cy * (cx + 1), nyf = (cy + 1) * cx, nzf = cy * cx;
+    const int pxs = (nxs + 31) & ~31, pys = (nys + 31) & ~31, pzs = (nzs + 31) & ~31;
+    const int pxf = (nxf + 31) & ~31, pyf = (nyf + 31) & ~31, pzf = (nzf + 31) & ~31;
+
     for (int k = kb; k < ke; k++) {
-      const R* pk = plane(k);
-      DivAcc<R> acc;
-      // ---- x pass ----
-      {
-        const int nsl = cy * (cx + 2);
-        for (int it = tid; it < nsl; it += NT) {
-          const int j = it / (cx + 2), i = it % (cx + 2) - 1;
-#pragma unroll
-          for (int n = 0; n < NPRIM; n++) {
-            const R m1 = PV(pk, n, i - 1, j), c0 = PV(pk, n, i, j), p1 = PV(pk, n, i + 1, j);
-            slp[(n * S::SY + (j + 1)) * SX + (i + 1)] = van_leer(p1 - c0, c0 - m1);
-          }
-        }
-        __syncthreads();
-        const int nf = cy * (cx + 1);
-        for (int it = tid; it < nf; it += NT) {
-          const int j = it / (cx + 1), i = it % (cx + 1);
-          R pl[NPRIM], pr[NPRIM], f[NCONS];
-#pragma unroll
-          for (int n = 0; n < NPRIM; n++) {
-            pl[n] = left_state(PV(pk, n, i - 1, j), slp[(n * S::SY + (j + 1)) * SX + i]);
-            pr[n] = right_state(PV(pk, n, i, j), slp[(n * S::SY + (j + 1)) * SX + (i + 1)]);
-          }
-          face_flux<R, 1>(pl, pr, chg, f);
-#pragma unroll
-          for (int m = 0; m < NCONS; m++) flx[(m * S::FY + j) * FX + i] = f[m];
-        }
-        __syncthreads();
-        if (own) {
-          const R xi = inv_of<R>(a.xinv, a.xinvf, ii + NGH);
-#pragma unroll
-          for (int m = 0; m < NCONS; m++)
-            acc.first(m, flx[(m * S::FY + ty) * FX + tx + 1] - flx[(m * S::FY + ty) * FX + tx], xi);
-        }
-        __syncthreads();
-      }
-      // ---- y pass ----
-      {
-        const int nsl = (cy + 2) * cx;
-        for (int it = tid; it < nsl; it += NT) {
-          const int j = it / cx - 1, i = it % cx;
-#pragma unroll
-          for (int n = 0; n < NPRIM; n++) {
-            const R m1 = PV(pk, n, i, j - 1), c0 = PV(pk, n, i, j), p1 = PV(pk, n, i, j + 1);
-            slp[(n * S::SY + (j + 1)) * SX + (i + 1)] = van_leer(p1 - c0, c0 - m1);
-          }
-        }
-        __syncthreads();
-        const int nf = (cy + 1) * cx;
-        for (int it = tid; it < nf; it += NT) {
-          const int j = it / cx, i = it % cx;
-          R pl[NPRIM], pr[NPRIM], f[NCONS];
-#pragma unroll
-          for (int n = 0; n < NPRIM; n++) {
-            pl[n] = left_state(PV(pk, n, i, j - 1), slp[(n * S::SY + j) * SX + (i + 1)]);
-            pr[n] = right_state(PV(pk, n, i, j), slp[(n * S::SY + (j + 1)) * SX + (i + 1)]);
-          }
-          face_flux<R, 2>(pl, pr, chg, f);
-#pragma unroll
-          for (int m = 0; m < NCONS; m++) flx[(m * S::FY + j) * FX + i] = f[m];
-        }
-        __syncthreads();
-        if (own) {
-          const R yi = inv_of<R>(a.yinv, a.yinvf, (a.quirk ? ii : jj) + NGH);
-#pragma unroll
-          for (int m = 0; m < NCONS; m++)
-            acc.add(m, flx[(m * S::FY + ty + 1) * FX + tx] - flx[(m * S::FY + ty) * FX + tx], yi);
-        }
-      }
-      // ---- z pass + update ----
       wait_plane(k + 2);
-      if (own && !s_abort) {
-        const R *p1 = plane(k + 1), *p2 = plane(k + 2);
-        R zs_nx[NPRIM], pl[NPRIM], pr[NPRIM], fz_hi[NCONS];
+      __syncthreads();
+      if (s_abort) break;
+      const R *pk = plane(k), *pk1 = plane(k + 1), *pk2 = plane(k + 2);
+      // ---- phase A: slopes ----
+      for (int q = tid; q < pxs + pys + pzs; q += NT) {
+        if (q < pxs) {
+          if (q < nxs) {
+            const int j = q / (cx + 2), i = q % (cx + 2) - 1;
 #pragma unroll
-        for (int n = 0; n < NPRIM; n++) {
-          const R c0 = PV(pk, n, tx, ty), c1 = PV(p1, n, tx, ty), c2 = PV(p2, n, tx, ty);
-          zs_nx[n] = van_leer(c2 - c1, c1 - c0);
-          pl[n] = left_state(c0, zs_cur[n]);
-          pr[n] = right_state(c1, zs_nx[n]);
+            for (int n = 0; n < NPRIM; n++) {
+              const R m1 = PV(pk, n, i - 1, j), c0 = PV(pk, n, i, j), p1 = PV(pk, n, i + 1, j);
+              SLX(n, i, j) = van_leer(p1 - c0, c0 - m1);
+            }
+          }
+        } else if (q < pxs + pys) {
+          const int r = q - pxs;
+          if (r < nys) {
+            const int j = r / cx - 1, i = r % cx;
+#pragma unroll
+            for (int n = 0; n < NPRIM; n++) {
+              const R m1 = PV(pk, n, i, j - 1), c0 = PV(pk, n, i, j), p1 = PV(pk, n, i, j + 1);
+              SLY(n, i, j) = van_leer(p1 - c0, c0 - m1);
+            }
+          }
+        } else {
+          const int r = q - pxs - pys;
+          if (r < nzs) {
+            const int j = r / cx, i = r % cx;
+#pragma unroll
+            for (int n = 0; n < NPRIM; n++) {
+              const R c0 = PV(pk, n, i, j), c1 = PV(pk1, n, i, j), c2 = PV(pk2, n, i, j);
+              SLZ(zb ^ 1, n, i, j) = van_leer(c2 - c1, c1 - c0);
+            }
+          }
         }
-        face_flux<R, 3>(pl, pr, chg, fz_hi);
-        const R zi = inv_of<R>(a.zinv, a.zinvf, (a.quirk ? ii : k) + NGH);
-        double u[NCONS];
+      }
+      __syncthreads();
+      // ---- phase B: face fluxes ----
+      for (int q = tid; q < pxf + pyf + pzf; q += NT) {
+        R pl[NPRIM], pr[NPRIM], f[NCONS];
+        if (q < pxf) {
+          if (q < nxf) {
+            const int j = q / (cx + 1), i = q % (cx + 1);
+#pragma unroll
+            for (int n = 0; n < NPRIM; n++) {
+              pl[n] = left_state(PV(pk, n, i - 1, j), SLX(n, i - 1, j));
+              pr[n] = right_state(PV(pk, n, i, j), SLX(n, i, j));
+            }
+            face_flux<R, 1>(pl, pr, chg, f);
+#pragma unroll
+            for (int m = 0; m < NCONS; m++) FXS(m, i, j) = f[m];
+          }
+        } else if (q < pxf + pyf) {
+          const int r = q - pxf;
+          if (r < nyf) {
+            const int j = r / cx, i = r % cx;
+#pragma unroll
+            for (int n = 0; n < NPRIM; n++) {
+              pl[n] = left_state(PV(pk, n, i, j - 1), SLY(n, i, j - 1));
+              pr[n] = right_state(PV(pk, n, i, j), SLY(n, i, j));
+            }
+            face_flux<R, 2>(pl, pr, chg, f);
+#pragma unroll
+            for (int m = 0; m < NCONS; m++) FYS(m, i, j) = f[m];
+          }
+        } else {
+          const int r = q - pxf - pyf;
+          if (r < nzf) {
+            const int j = r / cx, i = r % cx;
+#pragma unroll
+            for (int n = 0; n < NPRIM; n++) {
+              pl[n] = left_state(PV(pk, n, i, j), SLZ(zb, n, i, j));
+              pr[n] = right_state(PV(pk1, n, i, j), SLZ(zb ^ 1, n, i, j));
+            }
+            face_flux<R, 3>(pl, pr, chg, f);
+#pragma unroll
+            for (int m = 0; m < NCONS; m++) FZS(m, i, j) = f[m];
+          }
+        }
+      }
+      __syncthreads();
+      // ---- phase C: cell update, recovery, ghost images, candidates ----
+      if (own) {
+        DivAcc<R> acc;
+        const R xi = inv_of<R>(a, 0, ii + NGH);
+        const R yi = inv_of<R>(a, 1, (a.quirk ? ii : jj) + NGH);
+        const R zi = inv_of<R>(a, 2, (a.quirk ? ii : k) + NGH);
 #pragma unroll
         for (int m = 0; m < NCONS; m++) {
-          acc.add(m, fz_hi[m] - fz_lo[m], zi);
-          const size_t c = L.at(NCONS, m, k + NGH, jj + NGH, ii + NGH);
-          u[m] = a.U[c] - dt * acc.total(m);
+          acc.first(m, FXS(m, oi + 1, oj) - FXS(m, oi, oj), xi);
+          acc.add(m, FYS(m, oi, oj + 1) - FYS(m, oi, oj), yi);
+          const R fzh = FZS(m, oi, oj);
+          acc.add(m, fzh - fz_lo[m], zi);
+          fz_lo[m] = fzh;
         }
-        // DampPsi (mhd.cpp:1628-1630)
-        double dhl = a.dxs[ii + NGH];
-        if (a.dys[jj + NGH] < dhl) dhl = a.dys[jj + NGH];
-        if (a.dzs[k + NGH] < dhl) dhl = a.dzs[k + NGH];
-        const double taui = 0.1 * chd / dhl;
-        u[mbps] = u[mbps] * (1.0 - dt * taui);
+        const size_t c0 = L.at(NCONS, 0, k + NGH, jj + NGH, ii + NGH);
+        double u[NCONS];
+        update_cell(acc, a.U + c0, fsU, dt, chd, dtf, chf, a, ii + NGH, jj + NGH, k + NGH, u);
 #pragma unroll
-        for (int m = 0; m < NCONS; m++) a.U[L.at(NCONS, m, k + NGH, jj + NGH, ii + NGH)] = u[m];
-        double dtc, chc;
-        recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, k, a.dxs[ii + NGH], a.dys[jj + NGH], a.dzs[k + NGH],
-                        dtc, chc, bad);
-        dmin = smin(dmin, dtc);
+        for (int m = 0; m < NCONS; m++) a.U[c0 + m * fsU] = u[m];
+        R dtc, chc;
+        recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, k, spacing_of<R>(a, 0, ii + NGH),
+                        spacing_of<R>(a, 1, jj + NGH), spacing_of<R>(a, 2, k + NGH), dtc, chc, bad);
+        cmin = smin(cmin, dtc);
         cmax = smax(cmax, chc);
-#pragma unroll
-        for (int n = 0; n < NPRIM; n++) zs_cur[n] = zs_nx[n];
-#pragma unroll
-        for (int m = 0; m < NCONS; m++) fz_lo[m] = fz_hi[m];
       }
-      __syncthreads();  // plane k retired
-      if (s_abort) break;
+      __syncthreads();  // plane k and the work buffers retired
       if (k + 4 <= ke + 1) {
         if (tid == 0) {
           fence_proxy_async();
@@ -360,6 +485,7 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
         }
         fills[slot_of(k + 4)]++;
       }
+      zb ^= 1;
     }
     if (s_abort) break;
     __syncthreads();
@@ -371,7 +497,7 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
       if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &ctrl->status);
   }
   if (bad) atomicOr(&ctrl->status, bad);
-  block_reduce_to_slot(dmin, cmax, red, next);
+  block_reduce_to_slot((double)cmin, (double)cmax, red, next);
   if (tid == 0) {
     __threadfence();
     const unsigned prev = atomicAdd(&ctrl->blocks_done, 1u);
@@ -389,62 +515,62 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
   }
 }
 
-// Recovery of P from U for the interior (+ ghost images) and the dt/c_h reduction into
-// ctrl->slot[step % 3]: the state a fused run starts from.
+// Recovery of P from U for the interior (+ ghost images) and the dt/c_h reduction into a slot:
+// the state a fused run starts from.
 template <class R>
-__global__ void k_recover(const double* __restrict__ U, void* P, Layout L, int bc0, int bc1, int bc2, int bc3,
-                          int bc4, int bc5, const double* __restrict__ dxs, const double* __restrict__ dys,
-                          const double* __restrict__ dzs, double gam, RedSlot* slot, unsigned* status) {
+__global__ void k_recover(FusedArgs a, int which, RedSlot* slot) {
   __shared__ double scratch[64];
-  const int bc[6] = {bc0, bc1, bc2, bc3, bc4, bc5};
+  const Layout L = a.L;
   const long long n = (long long)L.nx * L.ny * L.nz;
-  double mn = 1.0e308, mx = 0.0;
+  R mn = R(1e30), mx = R(0);
   unsigned bad = 0;
-  R* Pout = reinterpret_cast<R*>(P);
+  R* Pout = reinterpret_cast<R*>(a.P[which]);
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int ii = (int)(t % L.nx), jj = (int)((t / L.nx) % L.ny), kk = (int)(t / ((long long)L.nx * L.ny));
     double u[NCONS];
 #pragma unroll
-    for (int m = 0; m < NCONS; m++) u[m] = U[L.at(NCONS, m, kk + NGH, jj + NGH, ii + NGH)];
-    double dtc, chc;
-    recover_cell<R>(u, gam, Pout, L, bc, ii, jj, kk, dxs[ii + NGH], dys[jj + NGH], dzs[kk + NGH], dtc, chc, bad);
+    for (int m = 0; m < NCONS; m++) u[m] = a.U[L.at(NCONS, m, kk + NGH, jj + NGH, ii + NGH)];
+    R dtc, chc;
+    recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, kk, spacing_of<R>(a, 0, ii + NGH), spacing_of<R>(a, 1, jj + NGH),
+                    spacing_of<R>(a, 2, kk + NGH), dtc, chc, bad);
     mn = smin(mn, dtc);
     mx = smax(mx, chc);
   }
-  if (bad) atomicOr(status, bad);
-  block_reduce_to_slot(mn, mx, scratch, slot);
+  if (bad) atomicOr(&a.ctrl->status, bad);
+  block_reduce_to_slot((double)mn, (double)mx, scratch, slot);
 }
 
 // Host side of one instantiation of the fused kernel.
-template <class R, int TX, int TY>
+template <class R, int TX, int TY, int NT>
 struct FusedLauncher {
-  using S = FusedSmem<R, TX, TY>;
-  static FusedShape shape() { return FusedShape{TX, TY, S::total, TX * TY, (int)sizeof(R)}; }
+  using S = FusedSmem<R, TX, TY, NT>;
+  static FusedShape shape() { return FusedShape{TX, TY, S::total, NT, (int)sizeof(R)}; }
   static cudaError_t prepare() {
-    return cudaFuncSetAttribute(k_fused_step<R, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::total);
+    return cudaFuncSetAttribute(k_fused_step<R, TX, TY, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)S::total);
   }
   static int ctas_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_fused_step<R, TX, TY>, TX * TY, S::total) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_fused_step<R, TX, TY, NT>, NT, S::total) != cudaSuccess)
       return 0;
     return n;
   }
   static cudaError_t launch(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s) {
-    k_fused_step<R, TX, TY><<<grid, TX * TY, S::total, s>>>(maps[0], maps[1], a);
+    k_fused_step<R, TX, TY, NT><<<grid, NT, S::total, s>>>(maps[0], maps[1], a);
     return cudaGetLastError();
+  }
+  static FusedVariant variant(FusedKind kind) {
+    return FusedVariant{kind, shape(), &prepare, &ctas_per_sm, &launch};
   }
 };
 
 template <class R>
-cudaError_t recover_launch(const double* U, void* P, const Layout& L, const int bc[6], const double* dxs,
-                           const double* dys, const double* dzs, double gam, RedSlot* slot, unsigned* status,
-                           int nsm, cudaStream_t s) {
+cudaError_t recover_launch(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
   const int bs = 256;
-  const long long n = (long long)L.nx * L.ny * L.nz;
+  const long long n = (long long)a.L.nx * a.L.ny * a.L.nz;
   long long g = (n + bs - 1) / bs;
   if (g > (long long)nsm * 8) g = (long long)nsm * 8;
-  k_recover<R><<<(unsigned)g, bs, 0, s>>>(U, P, L, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], dxs, dys, dzs, gam,
-                                          slot, status);
+  k_recover<R><<<(unsigned)g, bs, 0, s>>>(a, which, slot);
   return cudaGetLastError();
 }
 

@@ -1,4 +1,5 @@
-// fused_args.h -- launch arguments and shared-memory plan of the fused step kernel.
+// fused_args.h -- launch arguments of the fused step kernel and the table entry describing one
+// compiled tile shape of it (used by the host-side autotuner).
 #pragma once
 
 #include "common.cuh"
@@ -15,38 +16,27 @@ struct FusedShape {
 };
 
 struct FusedArgs {
-  double* U;                      // conserved state, NCONS fields
-  void* P[2];                     // primitive buffers (type R), NPRIM fields, step parity selects
+  double* U;                           // conserved state, NCONS fields
+  void* P[2];                          // primitive buffers (R), NPRIM fields; step parity selects
   Layout L;
-  const double *xinv, *yinv, *zinv;  // 1/(x?a(i+1)-x?a(i)) per index of the reference index space
-  const double *dxs, *dys, *dzs;     // x?a(i+1)-x?a(i)
-  const float *xinvf, *yinvf, *zinvf;  // the inverse spacings rounded to FP32 (mixed form)
+  const double *xinv, *yinv, *zinv;    // 1/(x?a(i+1)-x?a(i)) per index of the reference index space
+  const double *dxs, *dys, *dzs;       // x?a(i+1)-x?a(i)
+  const float *xinvf, *yinvf, *zinvf;  // the same rounded to FP32 (mixed form)
+  const float *dxsf, *dysf, *dzsf;
   double gam, cfl;
   int bc[6];
-  int quirk;                      // y/z inverse spacing taken at index i (mhd.cpp:1435-1436)
-  int ntx, nty, nkc, kc;          // tiles in x, y; chunks in z; planes per chunk
+  int quirk;                           // y/z inverse spacing taken at index i (mhd.cpp:1435-1436)
+  int ntx, nty, nkc, kc;               // tiles in x, y; chunks in z; planes per chunk
   Ctrl* ctrl;
 };
 
-template <class R, int TX, int TY>
-struct FusedSmem {
-  static constexpr int NBUF = 4;
-  static constexpr int PX = TX + 4, PY = TY + 4;
-  static constexpr int PLANE = PX * NPRIM * PY;               // elements of one ring plane
-  static constexpr int SX = TX + 2, SY = TY + 2;              // slope buffer extents
-  static constexpr int FX = TX + 1, FY = TY + 1;              // face-flux buffer extents
-  static constexpr size_t ring_bytes = (size_t)NBUF * PLANE * sizeof(R);
-  static constexpr size_t slope_bytes = (size_t)NPRIM * SY * SX * sizeof(R);
-  static constexpr size_t flux_bytes = (size_t)NCONS * FY * FX * sizeof(R);
-  static constexpr size_t ring_off = 0;
-  static constexpr size_t slope_off = (ring_bytes + 127) / 128 * 128;
-  static constexpr size_t flux_off = slope_off + (slope_bytes + 15) / 16 * 16;
-  static constexpr size_t red_off = flux_off + (flux_bytes + 15) / 16 * 16;
-  static constexpr size_t bar_off = red_off + 64 * sizeof(double);
-  static constexpr size_t misc_off = bar_off + NBUF * sizeof(uint64_t);  // work item, abort flag
-  static constexpr size_t used = misc_off + 16;
-  static constexpr size_t total = used + 128;  // room to align the base to 128 bytes
-  static constexpr unsigned plane_tx_bytes = (unsigned)(PLANE * sizeof(R));
+// One compiled instantiation of the fused kernel.
+struct FusedVariant {
+  FusedKind kind;
+  FusedShape shape;
+  cudaError_t (*prepare)();    // set the kernel's shared-memory attribute on the current device
+  int (*ctas_per_sm)();        // occupancy
+  cudaError_t (*launch)(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s);
 };
 
 }  // namespace mhdgb

@@ -24,26 +24,20 @@ cudaError_t launch_slot_to_scalars(const RedSlot* slot, double cfl, double* dt, 
 size_t pack_buffer_doubles(const Layout& L);
 cudaError_t launch_ghost_fill(double* P, const Layout& L, const int bc[6], double* scratch, cudaStream_t s);
 
-// ---- fused step (stages.cu: FP64 bit-exact; fast.cu: FP64 and mixed with FMA contraction) ----
-FusedShape fused_shape(FusedKind kind);
-// Sets the kernel attributes (dynamic shared memory); call once per device before launching.
-cudaError_t fused_prepare(FusedKind kind);
-// Occupancy: CTAs of the fused kernel resident per SM.
-int fused_ctas_per_sm(FusedKind kind);
-cudaError_t launch_fused(FusedKind kind, const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s);
-// Recover P (FP64 for FP64 kinds, FP32 for mixed) + ghost images from U; reduce dt/c_h into slot.
-cudaError_t launch_recover(FusedKind kind, const double* U, void* P, const Layout& L, const int bc[6],
-                           const double* dxs, const double* dys, const double* dzs, double gam, RedSlot* slot,
-                           unsigned* status, int nsm, cudaStream_t s);
+// ---- fused step ----
+// Compiled tile shapes of each kind (stages.cu: bit-exact FP64; fp64.cu: FP64; mixed.cu: mixed).
+int fused_variants(FusedKind kind, const FusedVariant** out);
+// Recover P (FP64 for FP64 kinds, FP32 for mixed) + ghost images from a.U into a.P[which];
+// reduce dt/c_h into slot.
+cudaError_t launch_recover(FusedKind kind, const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
 
-namespace detail {  // the bit-exact FP64 instantiation, compiled in stages.cu
-FusedShape exact_shape();
-cudaError_t exact_prepare();
-int exact_ctas_per_sm();
-cudaError_t exact_launch(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s);
-cudaError_t exact_recover(const double* U, void* P, const Layout& L, const int bc[6], const double* dxs,
-                          const double* dys, const double* dzs, double gam, RedSlot* slot, unsigned* status,
-                          int nsm, cudaStream_t s);
+namespace detail {
+int variants_exact(const FusedVariant** out);
+int variants_fp64(const FusedVariant** out);
+int variants_mixed(const FusedVariant** out);
+cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
+cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
+cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
 }  // namespace detail
 
 }  // namespace mhdgb

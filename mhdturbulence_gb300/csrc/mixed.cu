@@ -1,0 +1,28 @@
+// mixed.cu -- the FP32-mixed fused step.  Built with fast FP32 division and square root
+// (-prec-div=false -prec-sqrt=false -ftz=true): those only touch the FP32 reconstruction and Riemann
+// solve; the FP64 state update and pressure recovery are unaffected, and the compensated sums use
+// explicitly rounded intrinsics.
+#define MHDGB_VNS v_mixed
+#include "fused.cuh"
+#include "kernels.h"
+
+namespace mhdgb {
+namespace detail {
+
+int variants_mixed(const FusedVariant** out) {
+  static const FusedVariant v[] = {
+      v_mixed::FusedLauncher<float, 32, 4, 128>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncher<float, 32, 8, 256>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncher<float, 16, 8, 128>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncher<float, 64, 4, 256>::variant(FUSED_MIXED),
+  };
+  *out = v;
+  return (int)(sizeof(v) / sizeof(v[0]));
+}
+
+cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
+  return v_mixed::recover_launch<float>(a, which, slot, nsm, s);
+}
+
+}  // namespace detail
+}  // namespace mhdgb

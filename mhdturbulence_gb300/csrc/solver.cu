@@ -9,8 +9,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/mhdgb.h"
@@ -99,7 +103,7 @@ struct mhdgb_solver {
   double* F[3] = {nullptr, nullptr, nullptr};
   double* pack = nullptr;
   double *xinv = nullptr, *yinv = nullptr, *zinv = nullptr, *dxs = nullptr, *dys = nullptr, *dzs = nullptr;
-  float *xinvf = nullptr, *yinvf = nullptr, *zinvf = nullptr;
+  float *xinvf = nullptr, *yinvf = nullptr, *zinvf = nullptr, *dxsf = nullptr, *dysf = nullptr, *dzsf = nullptr;
   double* scal = nullptr;   // [0] dt, [1] chg of the stage path, [2..4] diagnostic, [8..] diag planes
   RedSlot* sslot = nullptr; // stage-path reduction slot
   Ctrl* ctrl = nullptr;
@@ -107,6 +111,8 @@ struct mhdgb_solver {
   // host state
   std::vector<double> x1a, x2a, x3a;
   CUtensorMap tmap[2];
+  const FusedVariant* vars = nullptr;  // compiled tile shapes of this precision
+  int nvars = 0, vidx = 0;             // and the one in use
   int grid = 0, ntx = 0, nty = 0, nkc = 0, kc = 0;
   long long cur_step = 0;    // device step count as of the last sync (selects the current P)
   bool have_state = false;   // U uploaded
@@ -189,8 +195,11 @@ int upload_grid(mhdgb_solver* h) {
   set_spacing_tables(h, dx, ix, h->x1a, n);
   set_spacing_tables(h, dy, iy, h->x2a, n);
   set_spacing_tables(h, dz, iz, h->x3a, n);
-  std::vector<float> fx(n), fy(n), fz(n);
-  for (int i = 0; i < n; i++) { fx[i] = (float)ix[i]; fy[i] = (float)iy[i]; fz[i] = (float)iz[i]; }
+  std::vector<float> fx(n), fy(n), fz(n), sx(n), sy(n), sz(n);
+  for (int i = 0; i < n; i++) {
+    fx[i] = (float)ix[i]; fy[i] = (float)iy[i]; fz[i] = (float)iz[i];
+    sx[i] = (float)dx[i]; sy[i] = (float)dy[i]; sz[i] = (float)dz[i];
+  }
   const size_t b = n * sizeof(double), bf = n * sizeof(float);
   CK(h, cudaMemcpy(h->dxs, dx.data(), b, cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->dys, dy.data(), b, cudaMemcpyHostToDevice));
@@ -201,6 +210,9 @@ int upload_grid(mhdgb_solver* h) {
   CK(h, cudaMemcpy(h->xinvf, fx.data(), bf, cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->yinvf, fy.data(), bf, cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->zinvf, fz.data(), bf, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->dxsf, sx.data(), bf, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->dysf, sy.data(), bf, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->dzsf, sz.data(), bf, cudaMemcpyHostToDevice));
   return MHDGB_OK;
 }
 
@@ -277,6 +289,7 @@ FusedArgs fused_args(mhdgb_solver* h) {
   a.xinv = h->xinv; a.yinv = h->yinv; a.zinv = h->zinv;
   a.dxs = h->dxs; a.dys = h->dys; a.dzs = h->dzs;
   a.xinvf = h->xinvf; a.yinvf = h->yinvf; a.zinvf = h->zinvf;
+  a.dxsf = h->dxsf; a.dysf = h->dysf; a.dzsf = h->dzsf;
   a.gam = h->cfg.gam;
   a.cfl = h->cfg.cfl;
   for (int q = 0; q < 6; q++) a.bc[q] = h->cfg.bc[q];
@@ -288,8 +301,69 @@ FusedArgs fused_args(mhdgb_solver* h) {
 
 int launch_one(mhdgb_solver* h) {
   FusedArgs a = fused_args(h);
-  CK(h, launch_fused(h->kind, h->tmap, a, h->grid, h->stream));
+  CK(h, h->vars[h->vidx].launch(h->tmap, a, h->grid, h->stream));
   return MHDGB_OK;
+}
+
+// Make variant idx the one in use: kernel attribute, grid, work decomposition, tensor maps.
+int use_variant(mhdgb_solver* h, int idx, int items_per_cta) {
+  if (idx < 0 || idx >= h->nvars) return fail(h, MHDGB_ERR_ARG, "no such variant");
+  const FusedVariant& v = h->vars[idx];
+  CK(h, v.prepare());
+  const int cps = v.ctas_per_sm();
+  if (cps < 1) return fail(h, MHDGB_ERR_CUDA, "fused kernel variant does not fit on an SM");
+  h->vidx = idx;
+  h->shape = v.shape;
+  h->grid = h->nsm * cps;
+  const Layout& L = h->L;
+  h->ntx = (L.nx + h->shape.tx - 1) / h->shape.tx;
+  h->nty = (L.ny + h->shape.ty - 1) / h->shape.ty;
+  // z chunks: about items_per_cta work items per CTA for load balance, chunks of >= 4 planes
+  const int tiles = h->ntx * h->nty;
+  int nkc = (items_per_cta * h->grid + tiles - 1) / tiles;
+  nkc = std::max(1, std::min(nkc, std::max(1, L.nz / 4)));
+  h->kc = (L.nz + nkc - 1) / nkc;
+  h->nkc = (L.nz + h->kc - 1) / h->kc;
+  void* pbase[2] = {h->kind == FUSED_MIXED ? (void*)h->P32[0] : (void*)h->P64[0],
+                    h->kind == FUSED_MIXED ? (void*)h->P32[1] : (void*)h->P64[1]};
+  int rc;
+  for (int q = 0; q < 2; q++)
+    if ((rc = make_tmap(h, &h->tmap[q], pbase[q], h->shape.elem))) return rc;
+  destroy_graph(h);
+  return MHDGB_OK;
+}
+
+// Process-wide autotune results: (kind, nx, ny, nz) -> variant index; optionally persisted in the
+// file named by MHDGB_TUNE_CACHE (lines "kind nx ny nz index").
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int>& tune_cache() {
+  static std::map<std::tuple<int, int, int, int>, int> m;
+  static bool loaded = false;
+  if (!loaded) {
+    loaded = true;
+    if (const char* f = std::getenv("MHDGB_TUNE_CACHE")) {
+      if (FILE* fp = std::fopen(f, "r")) {
+        int k, x, y, z, i;
+        while (std::fscanf(fp, "%d %d %d %d %d", &k, &x, &y, &z, &i) == 5) m[std::make_tuple(k, x, y, z)] = i;
+        std::fclose(fp);
+      }
+    }
+  }
+  return m;
+}
+
+void tune_cache_store(int kind, const Layout& L, int idx) {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  auto& m = tune_cache();
+  m[std::make_tuple(kind, L.nx, L.ny, L.nz)] = idx;
+  if (const char* f = std::getenv("MHDGB_TUNE_CACHE")) {
+    if (FILE* fp = std::fopen(f, "w")) {
+      for (auto& kv : m)
+        std::fprintf(fp, "%d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
+                     std::get<3>(kv.first), kv.second);
+      std::fclose(fp);
+    }
+  }
 }
 
 int build_graph(mhdgb_solver* h, int nsteps) {
@@ -360,7 +434,7 @@ int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
   int rc = set_device(h);
   if (rc) { delete h; return rc; }
   h->kind = cfg->precision == MHDGB_MIXED ? FUSED_MIXED : (cfg->precision == MHDGB_FP64_EXACT ? FUSED_FP64_EXACT : FUSED_FP64);
-  h->shape = fused_shape(h->kind);
+  h->nvars = fused_variants(h->kind, &h->vars);
   Layout& L = h->L;
   L.nx = cfg->nx; L.ny = cfg->ny; L.nz = cfg->nz;
   L.itot = cfg->nx + 2 * NGH + 1; L.jtot = cfg->ny + 2 * NGH + 1; L.ktot = cfg->nz + 2 * NGH + 1;
@@ -381,7 +455,8 @@ int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
        dalloc(h, &h->zinv, nmax) == cudaSuccess && dalloc(h, &h->dxs, nmax) == cudaSuccess &&
        dalloc(h, &h->dys, nmax) == cudaSuccess && dalloc(h, &h->dzs, nmax) == cudaSuccess &&
        dalloc(h, &h->xinvf, nmax) == cudaSuccess && dalloc(h, &h->yinvf, nmax) == cudaSuccess &&
-       dalloc(h, &h->zinvf, nmax) == cudaSuccess;
+       dalloc(h, &h->zinvf, nmax) == cudaSuccess && dalloc(h, &h->dxsf, nmax) == cudaSuccess &&
+       dalloc(h, &h->dysf, nmax) == cudaSuccess && dalloc(h, &h->dzsf, nmax) == cudaSuccess;
   ok = ok && dalloc(h, &h->scal, 8 + 3 * (size_t)L.nz) == cudaSuccess;
   ok = ok && dalloc(h, &h->sslot, 1) == cudaSuccess && dalloc(h, &h->ctrl, 1) == cudaSuccess;
   if (!ok) return cleanup(MHDGB_ERR_NOMEM);
@@ -389,21 +464,14 @@ int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
   h->x2a = face_axis(cfg->ny, cfg->x2min, cfg->x2max);
   h->x3a = face_axis(cfg->nz, cfg->x3min, cfg->x3max);
   if ((rc = upload_grid(h))) return cleanup(rc);
-  if (fused_prepare(h->kind) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
-  const int cps = std::max(1, fused_ctas_per_sm(h->kind));
-  h->grid = h->nsm * cps;
-  h->ntx = (L.nx + h->shape.tx - 1) / h->shape.tx;
-  h->nty = (L.ny + h->shape.ty - 1) / h->shape.ty;
-  // z chunks: aim for >= 4 work items per CTA for load balance, chunks of >= 4 planes
-  const int tiles = h->ntx * h->nty;
-  int nkc = (4 * h->grid + tiles - 1) / tiles;
-  nkc = std::max(1, std::min(nkc, L.nz / 4 > 0 ? L.nz / 4 : 1));
-  h->kc = (L.nz + nkc - 1) / nkc;
-  h->nkc = (L.nz + h->kc - 1) / h->kc;
-  void* pbase[2] = {h->kind == FUSED_MIXED ? (void*)h->P32[0] : (void*)h->P64[0],
-                    h->kind == FUSED_MIXED ? (void*)h->P32[1] : (void*)h->P64[1]};
-  for (int q = 0; q < 2; q++)
-    if ((rc = make_tmap(h, &h->tmap[q], pbase[q], h->shape.elem))) return cleanup(rc);
+  {
+    int idx = 0;
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto& m = tune_cache();
+    auto it = m.find(std::make_tuple((int)h->kind, L.nx, L.ny, L.nz));
+    if (it != m.end() && it->second < h->nvars) idx = it->second;
+    if ((rc = use_variant(h, idx, 4))) return cleanup(rc);
+  }
   k_ctrl_reset<<<1, 1, 0, h->stream>>>(h->ctrl, 0);
   k_ctrl_set_stop<<<1, 1, 0, h->stream>>>(h->ctrl, 1.0e300, ~0ull);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
@@ -418,7 +486,7 @@ int mhdgb_destroy(mhdgb_solver* h) {
   destroy_graph(h);
   void* ptrs[] = {h->U, h->P64[0], h->P64[1], h->P32[0], h->P32[1], h->F[0], h->F[1], h->F[2], h->pack,
                   h->xinv, h->yinv, h->zinv, h->dxs, h->dys, h->dzs, h->xinvf, h->yinvf, h->zinvf,
-                  h->scal, h->sslot, h->ctrl};
+                  h->dxsf, h->dysf, h->dzsf, h->scal, h->sslot, h->ctrl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -614,11 +682,10 @@ int mhdgb_prepare(mhdgb_solver* h) {
   if ((rc = read_ctrl(h, &c))) return rc;
   h->cur_step = (long long)c.step;
   const int cur = cur_index(h);
-  void* P = h->kind == FUSED_MIXED ? (void*)h->P32[cur] : (void*)h->P64[cur];
   CK(h, launch_reset_slot(&h->ctrl->slot[c.step % 3], h->stream));
   CK(h, launch_reset_slot(&h->ctrl->slot[(c.step + 1) % 3], h->stream));
-  CK(h, launch_recover(h->kind, h->U, P, h->L, h->cfg.bc, h->dxs, h->dys, h->dzs, h->cfg.gam,
-                       &h->ctrl->slot[c.step % 3], &h->ctrl->status, h->nsm, h->stream));
+  FusedArgs a = fused_args(h);
+  CK(h, launch_recover(h->kind, a, cur, &h->ctrl->slot[c.step % 3], h->nsm, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   h->prepared = true;
   h->p64_valid = h->kind != FUSED_MIXED;
@@ -737,6 +804,59 @@ int mhdgb_time_steps(mhdgb_solver* h, int nsteps, double* ms) {
   cudaEventDestroy(e1);
   *ms = t;
   return rc;
+}
+
+int mhdgb_variant_count(const mhdgb_solver* h) { return h ? h->nvars : 0; }
+
+int mhdgb_variant_info(const mhdgb_solver* h, int idx, int* tx, int* ty, int* threads, int* current) {
+  if (!h || idx < 0 || idx >= h->nvars) return MHDGB_ERR_ARG;
+  if (tx) *tx = h->vars[idx].shape.tx;
+  if (ty) *ty = h->vars[idx].shape.ty;
+  if (threads) *threads = h->vars[idx].shape.threads;
+  if (current) *current = idx == h->vidx;
+  return MHDGB_OK;
+}
+
+int mhdgb_select_variant(mhdgb_solver* h, int idx) {
+  if (!h) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = mhdgb_sync(h, nullptr)) == MHDGB_ERR_CUDA) return rc;
+  const bool was_prepared = h->prepared;
+  if ((rc = use_variant(h, idx, 4))) return rc;
+  h->prepared = was_prepared;  // the P buffers and reduction slots do not depend on the tile shape
+  return MHDGB_OK;
+}
+
+int mhdgb_autotune(mhdgb_solver* h, int steps, int* best) {
+  if (!h || steps < 1) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "autotune needs an uploaded state");
+  Ctrl saved;
+  if ((rc = read_ctrl(h, &saved))) return rc;
+  const size_t ub = h->L.count(NCONS) * sizeof(double);
+  CK(h, cudaMemcpyAsync(h->F[0], h->U, ub, cudaMemcpyDeviceToDevice, h->stream));  // F[0] has U's size
+  auto restore = [&]() -> int {
+    CK(h, cudaMemcpyAsync(h->U, h->F[0], ub, cudaMemcpyDeviceToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->cur_step = (long long)saved.step;
+    h->prepared = false;
+    h->p64_valid = false;
+    return MHDGB_OK;
+  };
+  double best_ms = 1e300;
+  int bidx = h->vidx;
+  for (int v = 0; v < h->nvars; v++) {
+    if ((rc = use_variant(h, v, 4)) || (rc = restore())) return rc;
+    double ms = 0.0;
+    if ((rc = mhdgb_time_steps(h, 2, &ms)) || (rc = mhdgb_time_steps(h, steps, &ms))) return rc;
+    if (ms < best_ms) { best_ms = ms; bidx = v; }
+  }
+  if ((rc = use_variant(h, bidx, 4)) || (rc = restore())) return rc;
+  tune_cache_store((int)h->kind, h->L, bidx);
+  if (best) *best = bidx;
+  return MHDGB_OK;
 }
 
 int mhdgb_diag(mhdgb_solver* h, double out[3]) {

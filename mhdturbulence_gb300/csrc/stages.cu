@@ -310,18 +310,32 @@ cudaError_t launch_ghost_fill(double* P, const Layout& L, const int bc[6], doubl
 }
 
 namespace detail {
-using ExactFP64 = v_exact::FusedLauncher<double, 32, 4>;
-FusedShape exact_shape() { return ExactFP64::shape(); }
-cudaError_t exact_prepare() { return ExactFP64::prepare(); }
-int exact_ctas_per_sm() { return ExactFP64::ctas_per_sm(); }
-cudaError_t exact_launch(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s) {
-  return ExactFP64::launch(maps, a, grid, s);
+int variants_exact(const FusedVariant** out) {
+  static const FusedVariant v[] = {
+      v_exact::FusedLauncher<double, 32, 4, 128>::variant(FUSED_FP64_EXACT),
+  };
+  *out = v;
+  return (int)(sizeof(v) / sizeof(v[0]));
 }
-cudaError_t exact_recover(const double* U, void* P, const Layout& L, const int bc[6], const double* dxs,
-                          const double* dys, const double* dzs, double gam, RedSlot* slot, unsigned* status,
-                          int nsm, cudaStream_t s) {
-  return v_exact::recover_launch<double>(U, P, L, bc, dxs, dys, dzs, gam, slot, status, nsm, s);
+cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
+  return v_exact::recover_launch<double>(a, which, slot, nsm, s);
 }
 }  // namespace detail
+
+int fused_variants(FusedKind kind, const FusedVariant** out) {
+  switch (kind) {
+    case FUSED_FP64_EXACT: return detail::variants_exact(out);
+    case FUSED_FP64: return detail::variants_fp64(out);
+    default: return detail::variants_mixed(out);
+  }
+}
+
+cudaError_t launch_recover(FusedKind kind, const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
+  switch (kind) {
+    case FUSED_FP64_EXACT: return detail::recover_exact(a, which, slot, nsm, s);
+    case FUSED_FP64: return detail::recover_fp64(a, which, slot, nsm, s);
+    default: return detail::recover_mixed(a, which, slot, nsm, s);
+  }
+}
 
 }  // namespace mhdgb

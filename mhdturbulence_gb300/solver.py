@@ -193,6 +193,24 @@ class Solver:
         self._ck(self._L.mhdgb_time_steps(self._h, n, C.byref(ms)), "time_steps")
         return ms.value
 
+    def variants(self):
+        """[(tx, ty, threads, current)] of the compiled fused-kernel tile shapes."""
+        out = []
+        for v in range(self._L.mhdgb_variant_count(self._h)):
+            tx, ty, nt, cur = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+            self._ck(self._L.mhdgb_variant_info(self._h, v, C.byref(tx), C.byref(ty), C.byref(nt), C.byref(cur)),
+                     "variant_info")
+            out.append((tx.value, ty.value, nt.value, bool(cur.value)))
+        return out
+
+    def select_variant(self, idx):
+        self._ck(self._L.mhdgb_select_variant(self._h, idx), "select_variant")
+
+    def autotune(self, steps=4) -> int:
+        best = C.c_int()
+        self._ck(self._L.mhdgb_autotune(self._h, steps, C.byref(best)), "autotune")
+        return best.value
+
     def diag(self):
         out = np.zeros(3)
         self._ck(self._L.mhdgb_diag(self._h, _dptr(out)), "diag")

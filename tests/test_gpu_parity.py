@@ -236,3 +236,48 @@ def test_init_kh_matches_python_generator():
         U = ic.interior(s.download_cons())
     Up = ic.interior(_kh_state(nx, ny, nz, seed=1))
     assert np.allclose(U, Up, rtol=1e-14, atol=1e-15)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_exact"])
+def test_every_tile_shape_gives_identical_results(precision):
+    # the per-cell arithmetic does not depend on the tile shape, so all compiled variants of one
+    # precision must agree bit for bit; an uneven grid exercises partial tiles and chunks
+    nx, ny, nz = 45, 22, 19
+    U0 = _kh_state(nx, ny, nz, seed=9)
+    outs = []
+    with Solver(nx, ny, nz, precision=precision) as s:
+        nvar = len(s.variants())
+    for v in range(nvar):
+        with Solver(nx, ny, nz, precision=precision) as s:
+            s.select_variant(v)
+            s.upload_cons(U0)
+            s.step(7)
+            r = s.sync()
+            assert r.step == 7
+            outs.append(s.download_cons())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_autotune_restores_state_and_is_remembered():
+    nx, ny, nz = 40, 32, 24
+    U0 = _kh_state(nx, ny, nz, seed=10)
+    with Solver(nx, ny, nz) as s:
+        s.upload_cons(U0)
+        s.step(3)
+        s.sync()
+        ref_state = s.download_cons()
+        best = s.autotune(steps=2)
+        assert 0 <= best < len(s.variants()) and s.variants()[best][3]
+        r = s.sync()
+        assert r.step == 3
+        assert np.array_equal(s.download_cons(), ref_state)
+        s.step(2)
+        s.sync()
+        after = s.download_cons()
+    with Solver(nx, ny, nz) as s2:
+        assert s2.variants()[best][3]  # remembered for the same grid and precision
+        s2.upload_cons(U0)
+        s2.step(5)
+        s2.sync()
+        assert np.array_equal(s2.download_cons(), after)
