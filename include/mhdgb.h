@@ -158,6 +158,10 @@ int mhdgb_select_variant(mhdgb_solver* h, int idx);
  * MHDGB_TUNE_CACHE names a file, across processes. */
 int mhdgb_autotune(mhdgb_solver* h, int steps, int* best);
 
+/* Measured FP64 FMA throughput of a device (GFLOP/s, 2 flops per FMA): the denominator of the
+ * FP64-pipe roofline of the FP64 form, which is bound by FP64 issue rather than by HBM. */
+int mhdgb_measure_fp64_rate(int device, double* gflops);
+
 /* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):
  * out = {volume, <X(1-X)>, sqrt(<v_y^2>)} over the interior, FP64 sums. */
 int mhdgb_diag(mhdgb_solver* h, double out[3]);

@@ -71,6 +71,7 @@ SIGNATURES = {
                                      C.POINTER(C.c_int)]),
     "mhdgb_select_variant": (C.c_int, [_vp, C.c_int]),
     "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
+    "mhdgb_measure_fp64_rate": (C.c_int, [C.c_int, _dp]),
     "mhdgb_diag": (C.c_int, [_vp, _dp]),
     "mhdgb_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double]),

@@ -75,9 +75,27 @@ __global__ void k_ctrl_set_stop(Ctrl* c, double tmax, unsigned long long max_ste
   c->done = (c->time > tmax || c->step >= max_step) ? 1u : 0u;
 }
 
-__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-    b[t] = (float)a[t];
+// Row repack between the dense host layout (row length itot) and the padded device pitch ip.
+__global__ void k_repack(const double* __restrict__ src, double* __restrict__ dst, int itot, int ip, size_t rows,
+                         int to_pitched) {
+  const size_t n = rows * (size_t)itot;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / itot, i = t % itot;
+    if (to_pitched) dst[r * ip + i] = src[t];
+    else dst[t] = src[r * ip + i];
+  }
+}
+
+// FP64 FMA issue-rate probe: 8 independent dependent-chains per thread, grid-strided.
+__global__ void k_dfma_rate(double* out, int iters) {
+  double a[8];
+  for (int i = 0; i < 8; i++) a[i] = 1.0 + 1e-9 * threadIdx.x + 0.01 * i;
+  for (int it = 0; it < iters; it++)
+#pragma unroll
+    for (int i = 0; i < 8; i++) a[i] = fma(a[i], 0.9999999, 1e-7);
+  double s = 0.0;
+  for (int i = 0; i < 8; i++) s += a[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
 uint64_t splitmix64(uint64_t x) {
@@ -118,6 +136,7 @@ struct mhdgb_solver {
   bool have_state = false;   // U uploaded
   bool prepared = false;     // fused buffers consistent with U
   bool p64_valid = false;    // P64[cur] holds the primitives of U (stage path view)
+  bool p_user = false;       // P64[cur] was uploaded by the caller and not superseded since
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
   std::string err;
@@ -247,9 +266,47 @@ int copy_d2h(mhdgb_solver* h, void* dst, const void* src, int nv, size_t elem) {
   return MHDGB_OK;
 }
 
+// Conserved-state transfers: one dense copy through a staging buffer, then a repack kernel (much
+// faster than a pitched 2-D copy with ~1 KB rows).  The staging buffer is the FP64 primitive buffer
+// that does not hold the current primitives (its 12 pitched fields exceed 10 dense ones); callers
+// synchronise first so that the current parity is known.
+double* staging(mhdgb_solver* h) { return h->P64[(h->cur_step & 1) ^ 1]; }
+
+int upload_u(mhdgb_solver* h, const double* U) {
+  const Layout& L = h->L;
+  const size_t rows = (size_t)NCONS * L.jtot * L.ktot;
+  double* st = staging(h);
+  CK(h, cudaMemcpyAsync(st, U, rows * L.itot * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  k_repack<<<h->nsm * 8, 256, 0, h->stream>>>(st, h->U, L.itot, L.ip, rows, 1);
+  CK(h, cudaGetLastError());
+  return MHDGB_OK;
+}
+
+int download_u(mhdgb_solver* h, double* U) {
+  const Layout& L = h->L;
+  const size_t rows = (size_t)NCONS * L.jtot * L.ktot;
+  double* st = staging(h);
+  k_repack<<<h->nsm * 8, 256, 0, h->stream>>>(h->U, st, L.itot, L.ip, rows, 0);
+  CK(h, cudaGetLastError());
+  CK(h, cudaMemcpyAsync(U, st, rows * L.itot * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return MHDGB_OK;
+}
+
 int read_ctrl(mhdgb_solver* h, Ctrl* c) {
   CK(h, cudaMemcpyAsync(c, h->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+// Wait for enqueued work and refresh the host's view of the step parity.
+int settle(mhdgb_solver* h) {
+  Ctrl c;
+  int rc = read_ctrl(h, &c);
+  if (rc) return rc;
+  if ((long long)c.step != h->cur_step) {
+    h->cur_step = (long long)c.step;
+    h->p64_valid = false;
+  }
   return MHDGB_OK;
 }
 
@@ -526,10 +583,10 @@ int mhdgb_set_grid(mhdgb_solver* h, const double* x1a, const double* x2a, const 
 int mhdgb_upload_cons(mhdgb_solver* h, const double* U) {
   if (!h || !U) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = copy_h2d(h, h->U, U, NCONS, sizeof(double)))) return rc;
+  if (rc || (rc = settle(h)) || (rc = upload_u(h, U))) return rc;
   h->have_state = true;
   h->prepared = false;
-  h->p64_valid = false;
+  h->p64_valid = h->p_user;  // a P the caller uploaded stays in force, as the reference's P array does
   CK(h, cudaStreamSynchronize(h->stream));
   return MHDGB_OK;
 }
@@ -537,8 +594,9 @@ int mhdgb_upload_cons(mhdgb_solver* h, const double* U) {
 int mhdgb_upload_prim(mhdgb_solver* h, const double* P) {
   if (!h || !P) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = copy_h2d(h, h->P64[cur_index(h)], P, NPRIM, sizeof(double)))) return rc;
+  if (rc || (rc = settle(h)) || (rc = copy_h2d(h, h->P64[cur_index(h)], P, NPRIM, sizeof(double)))) return rc;
   h->p64_valid = true;
+  h->p_user = true;
   h->prepared = false;
   CK(h, cudaStreamSynchronize(h->stream));
   return MHDGB_OK;
@@ -547,7 +605,7 @@ int mhdgb_upload_prim(mhdgb_solver* h, const double* P) {
 int mhdgb_download_cons(mhdgb_solver* h, double* U) {
   if (!h || !U) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = copy_d2h(h, U, h->U, NCONS, sizeof(double)))) return rc;
+  if (rc || (rc = settle(h)) || (rc = download_u(h, U))) return rc;
   CK(h, cudaStreamSynchronize(h->stream));
   return MHDGB_OK;
 }
@@ -652,6 +710,7 @@ int mhdgb_update_prim(mhdgb_solver* h) {
   CK(h, launch_update_prim(h->U, h->P64[cur_index(h)], h->L, h->cfg.gam, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   h->p64_valid = true;
+  h->p_user = false;
   h->prepared = false;
   return MHDGB_OK;
 }
@@ -706,6 +765,7 @@ int mhdgb_step(mhdgb_solver* h, int nsteps) {
   for (; nsteps > 0; nsteps--)
     if ((rc = launch_one(h))) return rc;
   h->p64_valid = false;
+  h->p_user = false;
   return MHDGB_OK;
 }
 
@@ -771,11 +831,12 @@ int mhdgb_reset_clock(mhdgb_solver* h) {
 int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nsteps, double* dt, double* chg) {
   if (!h || !U_in || !U_out || nsteps < 1) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = copy_h2d(h, h->U, U_in, NCONS, sizeof(double)))) return rc;
+  if (rc || (rc = settle(h)) || (rc = upload_u(h, U_in))) return rc;
   h->have_state = true;
   h->prepared = false;
+  h->p_user = false;
   if ((rc = mhdgb_prepare(h)) || (rc = mhdgb_step(h, nsteps))) return rc;
-  if ((rc = copy_d2h(h, U_out, h->U, NCONS, sizeof(double)))) return rc;
+  if ((rc = settle(h)) || (rc = download_u(h, U_out))) return rc;
   mhdgb_report rep;
   rc = mhdgb_sync(h, &rep);
   if (dt) *dt = rep.dt;
@@ -804,6 +865,38 @@ int mhdgb_time_steps(mhdgb_solver* h, int nsteps, double* ms) {
   cudaEventDestroy(e1);
   *ms = t;
   return rc;
+}
+
+int mhdgb_measure_fp64_rate(int device, double* gflops) {
+  if (!gflops) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  const int bs = 256, grid = nsm * 8, iters = 4000;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * grid * bs) != cudaSuccess) return MHDGB_ERR_NOMEM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dfma_rate<<<grid, bs>>>(out, 50);
+  cudaDeviceSynchronize();
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; rep++) {
+    cudaEventRecord(e0);
+    k_dfma_rate<<<grid, bs>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  const cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return MHDGB_ERR_CUDA;
+  *gflops = 2.0 * 8.0 * iters * (double)grid * bs / (best * 1e-3) / 1e9;  // 2 flops per FMA
+  return MHDGB_OK;
 }
 
 int mhdgb_variant_count(const mhdgb_solver* h) { return h ? h->nvars : 0; }

@@ -281,3 +281,27 @@ def test_autotune_restores_state_and_is_remembered():
         s2.step(5)
         s2.sync()
         assert np.array_equal(s2.download_cons(), after)
+
+
+def test_state_transfers_round_trip_exactly():
+    nx, ny, nz = 13, 9, 7
+    rng = np.random.default_rng(0)
+    with Solver(nx, ny, nz) as s:
+        U = rng.standard_normal((s.ktot, s.jtot, 10, s.itot))
+        P = rng.standard_normal((s.ktot, s.jtot, 12, s.itot))
+        s.upload_cons(U)
+        s.upload_prim(P)
+        assert np.array_equal(s.download_cons(), U)
+        assert np.array_equal(s.download_prim(), P)
+
+
+def test_reference_style_upload_of_p_and_u():
+    # GenerateProblem fills both P and U (main.cpp:93-183); a P the caller uploads is the one the
+    # first stage step uses, even when U is uploaded after it
+    case = next(c for c in CASES if c.full)
+    with solver_for(case, "fp64_exact") as s:
+        s.upload_prim(case.z["P0"])
+        s.upload_cons(case.U0())
+        dt, chg = s.stage_step()
+        assert dt == case.z["dts"][0] and chg == case.z["chgs"][0]
+        assert np.array_equal(s.download_cons(), case.z["U1"])
