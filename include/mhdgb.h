@@ -172,6 +172,29 @@ int mhdgb_diag(mhdgb_solver* h, double out[3]);
 int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, double width, double bx, double amp,
                   double sig, double noise);
 
+/* ---- ensemble: many independent grids advanced together ----
+ * Every member is an ordinary handle (upload/download/init/diag work on it; the ensemble owns it)
+ * with its own grid, boundaries, gam and state; all members share one stream and one precision.
+ * Each ensemble step is one persistent launch of the fused kernel that walks the work items of all
+ * members, every member advancing by its own dt; launches are captured in a CUDA graph. */
+typedef struct mhdgb_ensemble mhdgb_ensemble;
+int mhdgb_ensemble_create(int n, const mhdgb_config* cfgs, mhdgb_ensemble** out);
+int mhdgb_ensemble_destroy(mhdgb_ensemble* e);
+const char* mhdgb_ensemble_last_error(const mhdgb_ensemble* e);
+int mhdgb_ensemble_size(const mhdgb_ensemble* e);
+int mhdgb_ensemble_member(mhdgb_ensemble* e, int i, mhdgb_solver** h);
+long long mhdgb_ensemble_cells(const mhdgb_ensemble* e);
+int mhdgb_ensemble_prepare(mhdgb_ensemble* e);
+int mhdgb_ensemble_step(mhdgb_ensemble* e, int nsteps);
+/* reports: array of size() entries or NULL. */
+int mhdgb_ensemble_sync(mhdgb_ensemble* e, mhdgb_report* reports);
+int mhdgb_ensemble_set_stop(mhdgb_ensemble* e, double tmax, long long max_steps);
+int mhdgb_ensemble_time_steps(mhdgb_ensemble* e, int nsteps, double* ms);
+int mhdgb_ensemble_select_variant(mhdgb_ensemble* e, int idx);
+int mhdgb_ensemble_variant(const mhdgb_ensemble* e);
+/* Times every compiled tile shape on the whole ensemble (states restored) and keeps the fastest. */
+int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,6 +6,7 @@ the seeded initial-condition generators.
 """
 from . import ic  # noqa: F401
 from ._lib import MhdgbError  # noqa: F401
+from .ensemble import Ensemble, kh_ensemble_specs  # noqa: F401
 from .solver import Solver  # noqa: F401
 
-__all__ = ["Solver", "MhdgbError", "ic"]
+__all__ = ["Solver", "Ensemble", "kh_ensemble_specs", "MhdgbError", "ic"]

@@ -75,6 +75,20 @@ SIGNATURES = {
     "mhdgb_diag": (C.c_int, [_vp, _dp]),
     "mhdgb_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double]),
+    "mhdgb_ensemble_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(_vp)]),
+    "mhdgb_ensemble_destroy": (C.c_int, [_vp]),
+    "mhdgb_ensemble_last_error": (C.c_char_p, [_vp]),
+    "mhdgb_ensemble_size": (C.c_int, [_vp]),
+    "mhdgb_ensemble_member": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "mhdgb_ensemble_cells": (C.c_longlong, [_vp]),
+    "mhdgb_ensemble_prepare": (C.c_int, [_vp]),
+    "mhdgb_ensemble_step": (C.c_int, [_vp, C.c_int]),
+    "mhdgb_ensemble_sync": (C.c_int, [_vp, C.POINTER(Report)]),
+    "mhdgb_ensemble_set_stop": (C.c_int, [_vp, C.c_double, C.c_longlong]),
+    "mhdgb_ensemble_time_steps": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_ensemble_select_variant": (C.c_int, [_vp, C.c_int]),
+    "mhdgb_ensemble_variant": (C.c_int, [_vp]),
+    "mhdgb_ensemble_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
 }
 
 

@@ -243,7 +243,7 @@ __device__ __forceinline__ void update_cell(const DivAcc<float>& acc, const doub
 
 template <class R, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT, 1)
-k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ CUtensorMap tmap1, FusedArgs a) {
+k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc) {
   using S = FusedSmem<R, TX, TY, NT>;
   constexpr int NBUF = S::NBUF, PX = S::PX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -260,26 +260,18 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
   int& s_item = *reinterpret_cast<int*>(smem + S::misc_off);
   int& s_abort = *reinterpret_cast<int*>(smem + S::misc_off + 4);
 
-  Ctrl* ctrl = a.ctrl;
-  if (ctrl->done) return;
-  const Layout L = a.L;
   const int tid = threadIdx.x;
-  const unsigned long long step = ctrl->step;
-  const int par = (int)(step & 1);
-  R* __restrict__ Pout = reinterpret_cast<R*>(a.P[par ^ 1]);
-  const CUtensorMap* tmap = par ? &tmap1 : &tmap0;
-  const RedSlot cur_slot = ctrl->slot[step % 3];
-  const double dt = a.cfl * bitsd(cur_slot.dtmin_bits);
-  const double chd = bitsd(cur_slot.chmax_bits);
-  const R chg = (R)chd;
-  const float dtf = (float)dt, chf = (float)chd;
-  RedSlot* next = &ctrl->slot[(step + 1) % 3];
-  if (blockIdx.x == 0 && tid == 0) {
-    ctrl->slot[(step + 2) % 3].dtmin_bits = DT_RESET;
-    ctrl->slot[(step + 2) % 3].chmax_bits = CH_RESET;
-  }
+  const int ninst = (int)lc->ninst, total = (int)lc->total_items;
+  // step n of a grid reduces into slot (n+1)%3; slot (n+2)%3 is reset here for the next launch
+  if (blockIdx.x == 0)
+    for (int q = tid; q < ninst; q += NT) {
+      Ctrl* c = desc[q].a.ctrl;
+      if (!c->done) {
+        c->slot[(c->step + 2) % 3].dtmin_bits = DT_RESET;
+        c->slot[(c->step + 2) % 3].chmax_bits = CH_RESET;
+      }
+    }
   if (tid == 0) {
-    prefetch_tensormap(tmap);
     for (int s = 0; s < NBUF; s++) mbar_init(&bars[s], 1);
     fence_mbar_init();
     s_abort = 0;
@@ -289,18 +281,38 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
   unsigned fills[NBUF];  // loads issued per slot (identical in every thread)
 #pragma unroll
   for (int s = 0; s < NBUF; s++) fills[s] = 0;
-
   const int oi = tid % TX, oj = tid / TX;  // owner column of this thread (if oj < TY)
-  R cmin = R(1e30), cmax = R(0);
-  unsigned bad = 0;
-  const int nitems = a.ntx * a.nty * a.nkc;
-  const size_t fsU = (size_t)L.ip;  // field stride of U in the (k, j, n, i) layout
 
   for (;;) {
-    if (tid == 0) s_item = (int)atomicAdd(&ctrl->work_next, 1u);
+    if (tid == 0) s_item = (int)atomicAdd(&lc->work_next, 1u);
     __syncthreads();
-    const int item = s_item;
-    if (item >= nitems || s_abort) break;
+    const int gitem = s_item;
+    if (gitem >= total || s_abort) break;
+    int inst = 0;  // the grid this work item belongs to
+    for (int lo = 0, hi = ninst - 1; lo <= hi;) {
+      const int mid = (lo + hi) >> 1;
+      if (desc[mid].item_begin <= gitem) { inst = mid; lo = mid + 1; } else hi = mid - 1;
+    }
+    const FusedArgs& a = desc[inst].a;
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->done) { __syncthreads(); continue; }
+    const Layout L = a.L;
+    const size_t fsU = (size_t)L.ip;  // field stride of U in the (k, j, n, i) layout
+    const unsigned long long step = ctrl->step;
+    const int par = (int)(step & 1);
+    R* __restrict__ Pout = reinterpret_cast<R*>(a.P[par ^ 1]);
+    const CUtensorMap* tmap = &desc[inst].tmap[par];
+    const RedSlot cur_slot = ctrl->slot[step % 3];
+    const double dt = a.cfl * bitsd(cur_slot.dtmin_bits);
+    const double chd = bitsd(cur_slot.chmax_bits);
+    const R chg = (R)chd;
+    const float dtf = (float)dt, chf = (float)chd;
+    RedSlot* next = &ctrl->slot[(step + 1) % 3];
+    R cmin = R(1e30), cmax = R(0);
+    unsigned bad = 0;
+    if (tid == 0) prefetch_tensormap(tmap);
+
+    const int item = gitem - desc[inst].item_begin;
     const int bxi = item % a.ntx, byi = (item / a.ntx) % a.nty, bki = item / (a.ntx * a.nty);
     const int i0 = bxi * TX, j0 = byi * TY;
     const int kb = bki * a.kc, ke = min(kb + a.kc, L.nz);
@@ -487,29 +499,33 @@ k_fused_step(const __grid_constant__ CUtensorMap tmap0, const __grid_constant__ 
       }
       zb ^= 1;
     }
+    if (bad) atomicOr(&ctrl->status, bad);
+    block_reduce_to_slot((double)cmin, (double)cmax, red, next);
     if (s_abort) break;
-    __syncthreads();
   }
 
   if (s_abort) {
     // drain: wait (bounded) for any load still in flight before leaving
     for (int s = 0; s < NBUF; s++)
-      if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &ctrl->status);
+      if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &desc[0].a.ctrl->status);
   }
-  if (bad) atomicOr(&ctrl->status, bad);
-  block_reduce_to_slot((double)cmin, (double)cmax, red, next);
   if (tid == 0) {
     __threadfence();
-    const unsigned prev = atomicAdd(&ctrl->blocks_done, 1u);
-    if (prev == gridDim.x - 1) {
+    const unsigned prev = atomicAdd(&lc->blocks_done, 1u);
+    if (prev == gridDim.x - 1) {  // last CTA: advance every live grid by one step
       __threadfence();
-      ctrl->last_dt = dt;
-      ctrl->last_ch = chd;
-      ctrl->time += dt;
-      ctrl->step = step + 1;
-      ctrl->work_next = 0;
-      ctrl->blocks_done = 0;
-      if (ctrl->time > ctrl->tmax || ctrl->step >= ctrl->max_step) ctrl->done = 1;
+      for (int q = 0; q < ninst; q++) {
+        Ctrl* c = desc[q].a.ctrl;
+        if (c->done) continue;
+        const double dtq = desc[q].a.cfl * bitsd(c->slot[c->step % 3].dtmin_bits);
+        c->last_dt = dtq;
+        c->last_ch = bitsd(c->slot[c->step % 3].chmax_bits);
+        c->time += dtq;
+        c->step += 1;
+        if (c->time > c->tmax || c->step >= c->max_step) c->done = 1;
+      }
+      lc->work_next = 0;
+      lc->blocks_done = 0;
       __threadfence();
     }
   }
@@ -555,8 +571,8 @@ struct FusedLauncher {
       return 0;
     return n;
   }
-  static cudaError_t launch(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s) {
-    k_fused_step<R, TX, TY, NT><<<grid, NT, S::total, s>>>(maps[0], maps[1], a);
+  static cudaError_t launch(const InstanceDesc* desc, LaunchCtrl* lc, int grid, cudaStream_t s) {
+    k_fused_step<R, TX, TY, NT><<<grid, NT, S::total, s>>>(desc, lc);
     return cudaGetLastError();
   }
   static FusedVariant variant(FusedKind kind) {

@@ -30,13 +30,30 @@ struct FusedArgs {
   Ctrl* ctrl;
 };
 
+// One grid of a launch: its arguments, the TMA maps of its two primitive buffers and its range of
+// the launch's work queue.  Kept in device memory (tensor maps need 64-byte alignment).
+struct alignas(64) InstanceDesc {
+  CUtensorMap tmap[2];
+  FusedArgs a;
+  int item_begin;   // first work item of this grid in the launch's queue
+  int nitems;       // ntx * nty * nkc
+};
+
+// Launch-wide control of the fused kernel: the work-queue head and the CTA completion counter.
+struct LaunchCtrl {
+  unsigned work_next;
+  unsigned blocks_done;
+  unsigned ninst;
+  unsigned total_items;
+};
+
 // One compiled instantiation of the fused kernel.
 struct FusedVariant {
   FusedKind kind;
   FusedShape shape;
   cudaError_t (*prepare)();    // set the kernel's shared-memory attribute on the current device
   int (*ctas_per_sm)();        // occupancy
-  cudaError_t (*launch)(const CUtensorMap maps[2], const FusedArgs& a, int grid, cudaStream_t s);
+  cudaError_t (*launch)(const InstanceDesc* desc, LaunchCtrl* lc, int grid, cudaStream_t s);
 };
 
 }  // namespace mhdgb

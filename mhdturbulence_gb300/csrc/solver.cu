@@ -139,6 +139,10 @@ struct mhdgb_solver {
   bool p_user = false;       // P64[cur] was uploaded by the caller and not superseded since
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
+  InstanceDesc* d_desc = nullptr;  // this grid as a one-instance launch of the fused kernel
+  LaunchCtrl* d_lc = nullptr;
+  double* stage = nullptr;         // dense host-layout staging buffer (allocated on first transfer)
+  bool own_stream = true;          // false for the members of an ensemble (they share its stream)
   std::string err;
 };
 
@@ -266,16 +270,21 @@ int copy_d2h(mhdgb_solver* h, void* dst, const void* src, int nv, size_t elem) {
   return MHDGB_OK;
 }
 
-// Conserved-state transfers: one dense copy through a staging buffer, then a repack kernel (much
-// faster than a pitched 2-D copy with ~1 KB rows).  The staging buffer is the FP64 primitive buffer
-// that does not hold the current primitives (its 12 pitched fields exceed 10 dense ones); callers
-// synchronise first so that the current parity is known.
-double* staging(mhdgb_solver* h) { return h->P64[(h->cur_step & 1) ^ 1]; }
+// State transfers: one dense copy through a staging buffer, then a repack kernel (much faster than
+// a pitched 2-D copy with ~1 KB rows).
+double* staging(mhdgb_solver* h) {
+  if (!h->stage) {
+    const size_t n = (size_t)NPRIM * h->L.itot * h->L.jtot * h->L.ktot;
+    if (dalloc(h, &h->stage, n) != cudaSuccess) return nullptr;
+  }
+  return h->stage;
+}
 
 int upload_u(mhdgb_solver* h, const double* U) {
   const Layout& L = h->L;
   const size_t rows = (size_t)NCONS * L.jtot * L.ktot;
   double* st = staging(h);
+  if (!st) return fail(h, MHDGB_ERR_NOMEM, "staging buffer");
   CK(h, cudaMemcpyAsync(st, U, rows * L.itot * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   k_repack<<<h->nsm * 8, 256, 0, h->stream>>>(st, h->U, L.itot, L.ip, rows, 1);
   CK(h, cudaGetLastError());
@@ -286,6 +295,7 @@ int download_u(mhdgb_solver* h, double* U) {
   const Layout& L = h->L;
   const size_t rows = (size_t)NCONS * L.jtot * L.ktot;
   double* st = staging(h);
+  if (!st) return fail(h, MHDGB_ERR_NOMEM, "staging buffer");
   k_repack<<<h->nsm * 8, 256, 0, h->stream>>>(h->U, st, L.itot, L.ip, rows, 0);
   CK(h, cudaGetLastError());
   CK(h, cudaMemcpyAsync(U, st, rows * L.itot * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -319,8 +329,23 @@ int status_to_code(mhdgb_solver* h, unsigned st) {
 
 int cur_index(const mhdgb_solver* h) { return (int)(h->cur_step & 1); }
 
+// Buffers of the stage path, allocated on first use.
+int ensure_stage_bufs(mhdgb_solver* h) {
+  const Layout& L = h->L;
+  for (int q = 0; q < 3; q++)
+    if (!h->F[q] && dalloc(h, &h->F[q], L.count(NCONS)) != cudaSuccess) return fail(h, MHDGB_ERR_NOMEM, "flux arrays");
+  if (!h->pack && dalloc(h, &h->pack, pack_buffer_doubles(L)) != cudaSuccess)
+    return fail(h, MHDGB_ERR_NOMEM, "pack buffers");
+  for (int q = 0; q < 2; q++)
+    if (!h->P64[q] && dalloc(h, &h->P64[q], L.count(NPRIM)) != cudaSuccess)
+      return fail(h, MHDGB_ERR_NOMEM, "FP64 primitive arrays");
+  return MHDGB_OK;
+}
+
 // Make P64[cur] the primitives of U (interior + ghosts), for the stage path and downloads.
 int ensure_p64(mhdgb_solver* h) {
+  int rc = ensure_stage_bufs(h);
+  if (rc) return rc;
   if (h->p64_valid) return MHDGB_OK;
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
   double* P = h->P64[cur_index(h)];
@@ -356,14 +381,36 @@ FusedArgs fused_args(mhdgb_solver* h) {
   return a;
 }
 
+InstanceDesc host_desc(mhdgb_solver* h, int item_begin) {
+  InstanceDesc d;
+  std::memset(&d, 0, sizeof(d));
+  d.tmap[0] = h->tmap[0];
+  d.tmap[1] = h->tmap[1];
+  d.a = fused_args(h);
+  d.item_begin = item_begin;
+  d.nitems = h->ntx * h->nty * h->nkc;
+  return d;
+}
+
+// The handle as a one-instance launch: descriptor and launch control in device memory.
+int upload_desc(mhdgb_solver* h) {
+  const InstanceDesc d = host_desc(h, 0);
+  const LaunchCtrl lc{0u, 0u, 1u, (unsigned)d.nitems};
+  CK(h, cudaMemcpyAsync(h->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(h->d_lc, &lc, sizeof(lc), cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
 int launch_one(mhdgb_solver* h) {
-  FusedArgs a = fused_args(h);
-  CK(h, h->vars[h->vidx].launch(h->tmap, a, h->grid, h->stream));
+  CK(h, h->vars[h->vidx].launch(h->d_desc, h->d_lc, h->grid, h->stream));
   return MHDGB_OK;
 }
 
 // Make variant idx the one in use: kernel attribute, grid, work decomposition, tensor maps.
-int use_variant(mhdgb_solver* h, int idx, int items_per_cta) {
+// kc_fixed > 0 sets the planes per work item directly (ensembles keep items of similar size);
+// otherwise the z chunks give about items_per_cta work items per CTA.
+int use_variant(mhdgb_solver* h, int idx, int items_per_cta, int kc_fixed = 0) {
   if (idx < 0 || idx >= h->nvars) return fail(h, MHDGB_ERR_ARG, "no such variant");
   const FusedVariant& v = h->vars[idx];
   CK(h, v.prepare());
@@ -379,7 +426,7 @@ int use_variant(mhdgb_solver* h, int idx, int items_per_cta) {
   const int tiles = h->ntx * h->nty;
   int nkc = (items_per_cta * h->grid + tiles - 1) / tiles;
   nkc = std::max(1, std::min(nkc, std::max(1, L.nz / 4)));
-  h->kc = (L.nz + nkc - 1) / nkc;
+  h->kc = kc_fixed > 0 ? std::min(kc_fixed, L.nz) : (L.nz + nkc - 1) / nkc;
   h->nkc = (L.nz + h->kc - 1) / h->kc;
   void* pbase[2] = {h->kind == FUSED_MIXED ? (void*)h->P32[0] : (void*)h->P64[0],
                     h->kind == FUSED_MIXED ? (void*)h->P32[1] : (void*)h->P64[1]};
@@ -387,7 +434,7 @@ int use_variant(mhdgb_solver* h, int idx, int items_per_cta) {
   for (int q = 0; q < 2; q++)
     if ((rc = make_tmap(h, &h->tmap[q], pbase[q], h->shape.elem))) return rc;
   destroy_graph(h);
-  return MHDGB_OK;
+  return upload_desc(h);
 }
 
 // Process-wide autotune results: (kind, nx, ny, nz) -> variant index; optionally persisted in the
@@ -477,7 +524,10 @@ const char* mhdgb_status_string(int s) {
 
 const char* mhdgb_last_error(const mhdgb_solver* h) { return h ? h->err.c_str() : "null handle"; }
 
-int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
+}  // extern "C"
+
+namespace {
+int create_impl(const mhdgb_config* cfg, cudaStream_t shared, mhdgb_solver** out) {
   if (!cfg || !out) return MHDGB_ERR_ARG;
   *out = nullptr;
   if (cfg->nx < 2 || cfg->ny < 2 || cfg->nz < 2) return MHDGB_ERR_ARG;
@@ -500,14 +550,21 @@ int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
   if (cudaGetDeviceProperties(&prop, cfg->device) != cudaSuccess) { delete h; return MHDGB_ERR_CUDA; }
   h->nsm = prop.multiProcessorCount;
   auto cleanup = [&](int code) { mhdgb_destroy(h); return code; };
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
+  if (shared) {
+    h->stream = shared;
+    h->own_stream = false;
+  } else if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    return cleanup(MHDGB_ERR_CUDA);
+  }
   const int nmax = std::max(L.itot, std::max(L.jtot, L.ktot));
+  // Working set of the fused step: U and the two primitive buffers of its precision.  The stage
+  // path's flux and pack buffers (and FP64 primitives for the mixed form) come on first use.
   bool ok = dalloc(h, &h->U, L.count(NCONS)) == cudaSuccess;
-  for (int q = 0; q < 2 && ok; q++) ok = dalloc(h, &h->P64[q], L.count(NPRIM)) == cudaSuccess;
   if (h->kind == FUSED_MIXED)
     for (int q = 0; q < 2 && ok; q++) ok = dalloc(h, &h->P32[q], L.count(NPRIM)) == cudaSuccess;
-  for (int q = 0; q < 3 && ok; q++) ok = dalloc(h, &h->F[q], L.count(NCONS)) == cudaSuccess;
-  ok = ok && dalloc(h, &h->pack, pack_buffer_doubles(L)) == cudaSuccess;
+  else
+    for (int q = 0; q < 2 && ok; q++) ok = dalloc(h, &h->P64[q], L.count(NPRIM)) == cudaSuccess;
+  ok = ok && dalloc(h, &h->d_desc, 1) == cudaSuccess && dalloc(h, &h->d_lc, 1) == cudaSuccess;
   ok = ok && dalloc(h, &h->xinv, nmax) == cudaSuccess && dalloc(h, &h->yinv, nmax) == cudaSuccess &&
        dalloc(h, &h->zinv, nmax) == cudaSuccess && dalloc(h, &h->dxs, nmax) == cudaSuccess &&
        dalloc(h, &h->dys, nmax) == cudaSuccess && dalloc(h, &h->dzs, nmax) == cudaSuccess &&
@@ -536,6 +593,12 @@ int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) {
   return MHDGB_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) { return create_impl(cfg, nullptr, out); }
+
 int mhdgb_destroy(mhdgb_solver* h) {
   if (!h) return MHDGB_OK;
   cudaSetDevice(h->cfg.device);
@@ -543,10 +606,10 @@ int mhdgb_destroy(mhdgb_solver* h) {
   destroy_graph(h);
   void* ptrs[] = {h->U, h->P64[0], h->P64[1], h->P32[0], h->P32[1], h->F[0], h->F[1], h->F[2], h->pack,
                   h->xinv, h->yinv, h->zinv, h->dxs, h->dys, h->dzs, h->xinvf, h->yinvf, h->zinvf,
-                  h->dxsf, h->dysf, h->dzsf, h->scal, h->sslot, h->ctrl};
+                  h->dxsf, h->dysf, h->dzsf, h->scal, h->sslot, h->ctrl, h->d_desc, h->d_lc, h->stage};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return MHDGB_OK;
 }
@@ -594,7 +657,9 @@ int mhdgb_upload_cons(mhdgb_solver* h, const double* U) {
 int mhdgb_upload_prim(mhdgb_solver* h, const double* P) {
   if (!h || !P) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = settle(h)) || (rc = copy_h2d(h, h->P64[cur_index(h)], P, NPRIM, sizeof(double)))) return rc;
+  if (rc || (rc = settle(h)) || (rc = ensure_stage_bufs(h)) ||
+      (rc = copy_h2d(h, h->P64[cur_index(h)], P, NPRIM, sizeof(double))))
+    return rc;
   h->p64_valid = true;
   h->p_user = true;
   h->prepared = false;
@@ -625,7 +690,7 @@ int mhdgb_download_prim(mhdgb_solver* h, double* P) {
 int mhdgb_download_flux(mhdgb_solver* h, int dir, double* F) {
   if (!h || !F || dir < 1 || dir > 3) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = copy_d2h(h, F, h->F[dir - 1], NCONS, sizeof(double)))) return rc;
+  if (rc || (rc = ensure_stage_bufs(h)) || (rc = copy_d2h(h, F, h->F[dir - 1], NCONS, sizeof(double)))) return rc;
   CK(h, cudaStreamSynchronize(h->stream));
   return MHDGB_OK;
 }
@@ -683,6 +748,7 @@ int mhdgb_update_conserv(mhdgb_solver* h) {
   if (!h) return MHDGB_ERR_ARG;
   int rc = set_device(h);
   if (rc) return rc;
+  if ((rc = ensure_stage_bufs(h))) return rc;
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
   CK(h, launch_update_conserv(h->F[0], h->F[1], h->F[2], h->U, h->L, h->xinv, h->yinv, h->zinv,
                               h->cfg.spacing_quirk, h->scal + 0, h->stream));
@@ -695,6 +761,7 @@ int mhdgb_damp_psi(mhdgb_solver* h) {
   if (!h) return MHDGB_ERR_ARG;
   int rc = set_device(h);
   if (rc) return rc;
+  if ((rc = ensure_stage_bufs(h))) return rc;
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
   CK(h, launch_damp_psi(h->U, h->L, h->dxs, h->dys, h->dzs, h->scal + 0, h->scal + 1, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
@@ -706,6 +773,7 @@ int mhdgb_update_prim(mhdgb_solver* h) {
   if (!h) return MHDGB_ERR_ARG;
   int rc = set_device(h);
   if (rc) return rc;
+  if ((rc = ensure_stage_bufs(h))) return rc;
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
   CK(h, launch_update_prim(h->U, h->P64[cur_index(h)], h->L, h->cfg.gam, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
@@ -927,10 +995,15 @@ int mhdgb_autotune(mhdgb_solver* h, int steps, int* best) {
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "autotune needs an uploaded state");
   Ctrl saved;
   if ((rc = read_ctrl(h, &saved))) return rc;
-  const size_t ub = h->L.count(NCONS) * sizeof(double);
-  CK(h, cudaMemcpyAsync(h->F[0], h->U, ub, cudaMemcpyDeviceToDevice, h->stream));  // F[0] has U's size
+  const Layout& L = h->L;
+  const size_t rows = (size_t)NCONS * L.jtot * L.ktot;
+  double* st = staging(h);
+  if (!st) return fail(h, MHDGB_ERR_NOMEM, "staging buffer");
+  k_repack<<<h->nsm * 8, 256, 0, h->stream>>>(h->U, st, L.itot, L.ip, rows, 0);  // keep U
+  CK(h, cudaGetLastError());
   auto restore = [&]() -> int {
-    CK(h, cudaMemcpyAsync(h->U, h->F[0], ub, cudaMemcpyDeviceToDevice, h->stream));
+    k_repack<<<h->nsm * 8, 256, 0, h->stream>>>(st, h->U, L.itot, L.ip, rows, 1);
+    CK(h, cudaGetLastError());
     CK(h, cudaMemcpyAsync(h->ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->cur_step = (long long)saved.step;
@@ -1008,6 +1081,277 @@ int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, doubl
         U[at(mst)] = rho * X;
       }
   return mhdgb_upload_cons(h, U.data());
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Ensemble: many independent grids (uneven sizes, own parameters) advanced together, one persistent
+// launch of the fused kernel per step walking all grids' work items.
+// ---------------------------------------------------------------------------------------------
+struct mhdgb_ensemble {
+  int device = 0;
+  FusedKind kind = FUSED_FP64;
+  cudaStream_t stream = nullptr;
+  int nsm = 0;
+  std::vector<mhdgb_solver*> m;
+  const FusedVariant* vars = nullptr;
+  int nvars = 0, vidx = 0, grid = 0;
+  int kc = 8;                       // planes per work item: similar-sized items across grids
+  InstanceDesc* d_desc = nullptr;
+  LaunchCtrl* d_lc = nullptr;
+  int total_items = 0;
+  cudaGraphExec_t gexec = nullptr;
+  std::string err;
+};
+
+namespace {
+
+int efail(mhdgb_ensemble* e, int code, const std::string& msg) {
+  if (e) e->err = msg;
+  return code;
+}
+
+#define ECK(e, call)                                                                      \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return efail((e), MHDGB_ERR_CUDA, std::string(#call) + ": " + \
+                                        cudaGetErrorString(e_));                          \
+  } while (0)
+
+int ens_member_rc(mhdgb_ensemble* e, int i, int rc) {
+  if (rc) e->err = "member " + std::to_string(i) + ": " + e->m[i]->err;
+  return rc;
+}
+
+// Use tile shape idx for every member and rebuild the launch's instance table.
+int ens_use_variant(mhdgb_ensemble* e, int idx) {
+  if (idx < 0 || idx >= e->nvars) return efail(e, MHDGB_ERR_ARG, "no such variant");
+  std::vector<InstanceDesc> d(e->m.size());
+  int begin = 0;
+  for (size_t i = 0; i < e->m.size(); i++) {
+    const bool was = e->m[i]->prepared;
+    int rc = use_variant(e->m[i], idx, 4, e->kc);
+    if (rc) return ens_member_rc(e, (int)i, rc);
+    e->m[i]->prepared = was;
+    d[i] = host_desc(e->m[i], begin);
+    begin += d[i].nitems;
+  }
+  e->vidx = idx;
+  e->total_items = begin;
+  e->grid = e->m[0]->grid;
+  const LaunchCtrl lc{0u, 0u, (unsigned)e->m.size(), (unsigned)begin};
+  ECK(e, cudaMemcpyAsync(e->d_desc, d.data(), d.size() * sizeof(InstanceDesc), cudaMemcpyHostToDevice, e->stream));
+  ECK(e, cudaMemcpyAsync(e->d_lc, &lc, sizeof(lc), cudaMemcpyHostToDevice, e->stream));
+  ECK(e, cudaStreamSynchronize(e->stream));
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  e->gexec = nullptr;
+  return MHDGB_OK;
+}
+
+int ens_launch(mhdgb_ensemble* e) {
+  ECK(e, e->vars[e->vidx].launch(e->d_desc, e->d_lc, e->grid, e->stream));
+  return MHDGB_OK;
+}
+
+int ens_prepare_all(mhdgb_ensemble* e, bool force) {
+  for (size_t i = 0; i < e->m.size(); i++) {
+    if (!force && e->m[i]->prepared) continue;
+    int rc = mhdgb_prepare(e->m[i]);
+    if (rc) return ens_member_rc(e, (int)i, rc);
+  }
+  return MHDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhdgb_ensemble_create(int n, const mhdgb_config* cfgs, mhdgb_ensemble** out) {
+  if (n < 1 || !cfgs || !out) return MHDGB_ERR_ARG;
+  *out = nullptr;
+  for (int i = 1; i < n; i++)
+    if (cfgs[i].precision != cfgs[0].precision || cfgs[i].device != cfgs[0].device) return MHDGB_ERR_ARG;
+  mhdgb_ensemble* e = new mhdgb_ensemble();
+  e->device = cfgs[0].device;
+  if (cudaSetDevice(e->device) != cudaSuccess) { delete e; return MHDGB_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) { delete e; return MHDGB_ERR_CUDA; }
+  cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->device);
+  for (int i = 0; i < n; i++) {
+    mhdgb_solver* h = nullptr;
+    int rc = create_impl(&cfgs[i], e->stream, &h);
+    if (rc) { mhdgb_ensemble_destroy(e); return rc; }
+    e->m.push_back(h);
+  }
+  e->kind = e->m[0]->kind;
+  e->vars = e->m[0]->vars;
+  e->nvars = e->m[0]->nvars;
+  if (cudaMalloc(&e->d_desc, n * sizeof(InstanceDesc)) != cudaSuccess ||
+      cudaMalloc(&e->d_lc, sizeof(LaunchCtrl)) != cudaSuccess) {
+    mhdgb_ensemble_destroy(e);
+    return MHDGB_ERR_NOMEM;
+  }
+  int rc = ens_use_variant(e, 0);
+  if (rc) { mhdgb_ensemble_destroy(e); return rc; }
+  *out = e;
+  return MHDGB_OK;
+}
+
+int mhdgb_ensemble_destroy(mhdgb_ensemble* e) {
+  if (!e) return MHDGB_OK;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  for (auto* h : e->m) mhdgb_destroy(h);
+  if (e->d_desc) cudaFree(e->d_desc);
+  if (e->d_lc) cudaFree(e->d_lc);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return MHDGB_OK;
+}
+
+const char* mhdgb_ensemble_last_error(const mhdgb_ensemble* e) { return e ? e->err.c_str() : "null ensemble"; }
+
+int mhdgb_ensemble_size(const mhdgb_ensemble* e) { return e ? (int)e->m.size() : 0; }
+
+int mhdgb_ensemble_member(mhdgb_ensemble* e, int i, mhdgb_solver** h) {
+  if (!e || !h || i < 0 || i >= (int)e->m.size()) return MHDGB_ERR_ARG;
+  *h = e->m[i];
+  return MHDGB_OK;
+}
+
+long long mhdgb_ensemble_cells(const mhdgb_ensemble* e) {
+  long long c = 0;
+  if (e)
+    for (auto* h : e->m) c += (long long)h->L.nx * h->L.ny * h->L.nz;
+  return c;
+}
+
+int mhdgb_ensemble_select_variant(mhdgb_ensemble* e, int idx) {
+  if (!e) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  ECK(e, cudaStreamSynchronize(e->stream));
+  return ens_use_variant(e, idx);
+}
+
+int mhdgb_ensemble_variant(const mhdgb_ensemble* e) { return e ? e->vidx : -1; }
+
+int mhdgb_ensemble_prepare(mhdgb_ensemble* e) {
+  if (!e) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  return ens_prepare_all(e, true);
+}
+
+int mhdgb_ensemble_step(mhdgb_ensemble* e, int nsteps) {
+  if (!e || nsteps < 0) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  int rc = ens_prepare_all(e, false);
+  if (rc) return rc;
+  const int G = 16;
+  if (nsteps >= G && !e->gexec) {
+    cudaGraph_t g = nullptr;
+    ECK(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < G && rc == MHDGB_OK; s++) rc = ens_launch(e);
+    cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (ce != cudaSuccess) return efail(e, MHDGB_ERR_CUDA, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&e->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return efail(e, MHDGB_ERR_CUDA, "cudaGraphInstantiate");
+  }
+  while (nsteps >= G) {
+    ECK(e, cudaGraphLaunch(e->gexec, e->stream));
+    nsteps -= G;
+  }
+  for (; nsteps > 0; nsteps--)
+    if ((rc = ens_launch(e))) return rc;
+  for (auto* h : e->m) { h->p64_valid = false; h->p_user = false; }
+  return MHDGB_OK;
+}
+
+int mhdgb_ensemble_sync(mhdgb_ensemble* e, mhdgb_report* reports) {
+  if (!e) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  int first = MHDGB_OK;
+  for (size_t i = 0; i < e->m.size(); i++) {
+    const int rc = mhdgb_sync(e->m[i], reports ? &reports[i] : nullptr);
+    if (rc && first == MHDGB_OK) first = ens_member_rc(e, (int)i, rc);
+  }
+  return first;
+}
+
+int mhdgb_ensemble_set_stop(mhdgb_ensemble* e, double tmax, long long max_steps) {
+  if (!e) return MHDGB_ERR_ARG;
+  for (size_t i = 0; i < e->m.size(); i++) {
+    const int rc = mhdgb_set_stop(e->m[i], tmax, max_steps);
+    if (rc) return ens_member_rc(e, (int)i, rc);
+  }
+  return MHDGB_OK;
+}
+
+int mhdgb_ensemble_time_steps(mhdgb_ensemble* e, int nsteps, double* ms) {
+  if (!e || nsteps < 1 || !ms) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  int rc = ens_prepare_all(e, false);
+  if (rc) return rc;
+  if (nsteps >= 16 && !e->gexec && (rc = mhdgb_ensemble_step(e, 0))) return rc;
+  cudaEvent_t e0, e1;
+  ECK(e, cudaEventCreate(&e0));
+  ECK(e, cudaEventCreate(&e1));
+  ECK(e, cudaStreamSynchronize(e->stream));
+  ECK(e, cudaEventRecord(e0, e->stream));
+  rc = mhdgb_ensemble_step(e, nsteps);
+  ECK(e, cudaEventRecord(e1, e->stream));
+  ECK(e, cudaEventSynchronize(e1));
+  float t = 0.0f;
+  ECK(e, cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t;
+  return rc;
+}
+
+int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best) {
+  if (!e || steps < 1) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  // keep every member's U and control block, time each tile shape, restore
+  std::vector<Ctrl> saved(e->m.size());
+  for (size_t i = 0; i < e->m.size(); i++) {
+    mhdgb_solver* h = e->m[i];
+    if (!h->have_state) return efail(e, MHDGB_ERR_STATE, "autotune needs every member's state");
+    int rc = read_ctrl(h, &saved[i]);
+    if (rc) return ens_member_rc(e, (int)i, rc);
+    double* st = staging(h);
+    if (!st) return efail(e, MHDGB_ERR_NOMEM, "staging buffer");
+    k_repack<<<h->nsm * 8, 256, 0, e->stream>>>(h->U, st, h->L.itot, h->L.ip,
+                                                 (size_t)NCONS * h->L.jtot * h->L.ktot, 0);
+    ECK(e, cudaGetLastError());
+  }
+  auto restore = [&]() -> int {
+    for (size_t i = 0; i < e->m.size(); i++) {
+      mhdgb_solver* h = e->m[i];
+      k_repack<<<h->nsm * 8, 256, 0, e->stream>>>(h->stage, h->U, h->L.itot, h->L.ip,
+                                                   (size_t)NCONS * h->L.jtot * h->L.ktot, 1);
+      ECK(e, cudaGetLastError());
+      ECK(e, cudaMemcpyAsync(h->ctrl, &saved[i], sizeof(Ctrl), cudaMemcpyHostToDevice, e->stream));
+      h->cur_step = (long long)saved[i].step;
+      h->prepared = false;
+      h->p64_valid = false;
+    }
+    ECK(e, cudaStreamSynchronize(e->stream));
+    return MHDGB_OK;
+  };
+  double best_ms = 1e300;
+  int bidx = e->vidx, rc;
+  for (int v = 0; v < e->nvars; v++) {
+    if ((rc = ens_use_variant(e, v)) || (rc = restore())) return rc;
+    double ms = 0.0;
+    if ((rc = mhdgb_ensemble_time_steps(e, 2, &ms)) || (rc = mhdgb_ensemble_time_steps(e, steps, &ms))) return rc;
+    if (ms < best_ms) { best_ms = ms; bidx = v; }
+  }
+  if ((rc = ens_use_variant(e, bidx)) || (rc = restore())) return rc;
+  if (best) *best = bidx;
+  return MHDGB_OK;
 }
 
 }  // extern "C"

@@ -14,6 +14,20 @@ from . import ic
 from ._lib import PRECISIONS, Config, MhdgbError, Report, lib
 
 
+def make_config(nx, ny, nz, domain=ic.KH_DOMAIN, bc=ic.KH_BC, gam=5.0 / 3.0, cfl=0.05, precision="fp64",
+                spacing_quirk=False, device=0) -> Config:
+    cfg = Config()
+    lib().mhdgb_config_default(C.byref(cfg))
+    cfg.nx, cfg.ny, cfg.nz = nx, ny, nz
+    (cfg.x1min, cfg.x1max), (cfg.x2min, cfg.x2max), (cfg.x3min, cfg.x3max) = domain
+    cfg.bc = (C.c_int * 6)(*bc)
+    cfg.gam, cfg.cfl = gam, cfl
+    cfg.precision = PRECISIONS[precision]
+    cfg.spacing_quirk = 1 if spacing_quirk else 0
+    cfg.device = device
+    return cfg
+
+
 def _dptr(a: np.ndarray):
     if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
         raise ValueError("arrays must be C-contiguous float64")
@@ -29,22 +43,23 @@ class Solver:
     taken at index i in UpdateConservU)."""
 
     def __init__(self, nx, ny, nz, domain=ic.KH_DOMAIN, bc=ic.KH_BC, gam=5.0 / 3.0, cfl=0.05,
-                 precision="fp64", spacing_quirk=False, device=0):
+                 precision="fp64", spacing_quirk=False, device=0, _borrow=None):
         self._L = lib()
-        cfg = Config()
-        self._L.mhdgb_config_default(C.byref(cfg))
-        cfg.nx, cfg.ny, cfg.nz = nx, ny, nz
-        (cfg.x1min, cfg.x1max), (cfg.x2min, cfg.x2max), (cfg.x3min, cfg.x3max) = domain
-        cfg.bc = (C.c_int * 6)(*bc)
-        cfg.gam, cfg.cfl = gam, cfl
-        cfg.precision = PRECISIONS[precision]
-        cfg.spacing_quirk = 1 if spacing_quirk else 0
-        cfg.device = device
+        self._owned = _borrow is None
+        cfg = make_config(nx, ny, nz, domain, bc, gam, cfl, precision, spacing_quirk, device)
+        if _borrow is not None:
+            self._h = _borrow
+            self._setup(nx, ny, nz, precision, cfg)
+            return
         h = C.c_void_p()
         rc = self._L.mhdgb_create(C.byref(cfg), C.byref(h))
         if rc != 0:
             raise MhdgbError(rc, "mhdgb_create failed")
         self._h = h
+        self._setup(nx, ny, nz, precision, cfg)
+
+    def _setup(self, nx, ny, nz, precision, cfg):
+        h = self._h
         self.nx, self.ny, self.nz = nx, ny, nz
         self.precision = precision
         self.cfg = cfg
@@ -60,7 +75,8 @@ class Solver:
 
     def close(self):
         if getattr(self, "_h", None):
-            self._L.mhdgb_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._L.mhdgb_destroy(self._h)
             self._h = None
 
     def __del__(self):

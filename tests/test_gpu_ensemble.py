@@ -1,0 +1,80 @@
+"""The batched ensemble form: every member of an ensemble advances exactly as the same grid run
+alone (same precision and tile shape: the per-cell arithmetic is identical), with its own dt."""
+import numpy as np
+import pytest
+
+from mhdturbulence_gb300 import Ensemble, Solver, ic, kh_ensemble_specs
+
+pytestmark = pytest.mark.gpu
+
+
+def _specs():
+    specs = kh_ensemble_specs(5, seed=7, sizes=(16, 24, 32))
+    # mixed boundaries and one periodic cube among the members
+    specs[1]["bc"] = (ic.BC_OUTFLOW, ic.BC_REFLECTION, ic.BC_PERIODIC, ic.BC_PERIODIC, ic.BC_REFLECTION,
+                      ic.BC_OUTFLOW)
+    specs[3]["bc"] = ic.PERIODIC_BC
+    specs[3]["domain"] = ic.CUBE_DOMAIN
+    return specs
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ensemble_members_match_single_grid_runs(precision):
+    specs = _specs()
+    nsteps = 21
+    with Ensemble(specs, precision=precision) as ens:
+        ens.init_kh()
+        U0 = [m.download_cons() for m in ens.members]
+        ens.step(nsteps)
+        reps = ens.sync()
+        out = [m.download_cons() for m in ens.members]
+        var = ens.variant
+    dts = set()
+    for sp, u0, u1, r in zip(specs, U0, out, reps):
+        assert r.step == nsteps
+        dts.add(r.dt)
+        with Solver(sp["nx"], sp["ny"], sp["nz"], precision=precision, domain=sp.get("domain", ic.KH_DOMAIN),
+                    bc=sp.get("bc", ic.KH_BC)) as s:
+            s.select_variant(var)
+            s.upload_cons(u0)
+            s.step(nsteps)
+            r1 = s.sync()
+            assert np.array_equal(s.download_cons(), u1)
+            assert r1.time == r.time
+    assert len(dts) == len(specs)  # every member moved by its own dt
+
+
+def test_ensemble_autotune_and_variants_agree():
+    specs = _specs()
+    results = []
+    with Ensemble(specs, precision="mixed") as ens:
+        ens.init_kh()
+        U0 = [m.download_cons() for m in ens.members]
+        best = ens.autotune(steps=2)
+        assert ens.variant == best
+        for m, u in zip(ens.members, U0):  # autotune restores every member
+            assert np.array_equal(m.download_cons(), u)
+        for v in range(len(ens.members[0].variants())):
+            ens.select_variant(v)
+            for m, u in zip(ens.members, U0):
+                m.upload_cons(u)
+                m.reset_clock()
+                m.upload_cons(u)
+            ens.step(5)
+            ens.sync()
+            results.append([m.download_cons() for m in ens.members])
+    for r in results[1:]:
+        for a, b in zip(r, results[0]):
+            assert np.array_equal(a, b)
+
+
+def test_ensemble_stop_condition_per_member():
+    specs = _specs()[:3]
+    with Ensemble(specs, precision="fp64") as ens:
+        ens.init_kh()
+        ens.set_stop(tmax=1e300, max_steps=4)
+        ens.members[1].set_stop(1e300, 2)
+        ens.step(6)
+        reps = ens.sync()
+        assert [r.step for r in reps] == [4, 2, 4]
+        assert all(r.done for r in reps)
