@@ -93,6 +93,10 @@ int mhdgb_extents(const mhdgb_solver* h, int* itot, int* jtot, int* ktot);
 /* Bytes of device memory held by the handle. */
 size_t mhdgb_device_bytes(const mhdgb_solver* h);
 
+/* Change gam (hydflux_mod::gam), the CFL factor and the boundary types (boundary_mod::boundary_xin
+ * ... _zout, boundary.cpp:26-31) of an existing handle; bc may be NULL to keep them. */
+int mhdgb_set_physics(mhdgb_solver* h, double gam, double cfl, const int* bc);
+
 /* GridArray G (mhd.hpp:22-182): cell faces x1a/x2a/x3a, lengths itot/jtot/ktot. */
 int mhdgb_get_grid(const mhdgb_solver* h, double* x1a, double* x2a, double* x3a);
 int mhdgb_set_grid(mhdgb_solver* h, const double* x1a, const double* x2a, const double* x3a);

@@ -42,6 +42,7 @@ SIGNATURES = {
     "mhdgb_status_string": (C.c_char_p, [C.c_int]),
     "mhdgb_extents": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "mhdgb_device_bytes": (C.c_size_t, [_vp]),
+    "mhdgb_set_physics": (C.c_int, [_vp, C.c_double, C.c_double, C.POINTER(C.c_int)]),
     "mhdgb_get_grid": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mhdgb_set_grid": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mhdgb_upload_cons": (C.c_int, [_vp, _dp]),

@@ -632,6 +632,25 @@ int mhdgb_get_grid(const mhdgb_solver* h, double* x1a, double* x2a, double* x3a)
   return MHDGB_OK;
 }
 
+int mhdgb_set_physics(mhdgb_solver* h, double gam, double cfl, const int* bc) {
+  if (!h || !(gam > 1.0) || !(cfl > 0.0)) return MHDGB_ERR_ARG;
+  if (bc)
+    for (int q = 0; q < 6; q++)
+      if (bc[q] < 1 || bc[q] > 3) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = settle(h))) return rc;
+  const bool same = h->cfg.gam == gam && h->cfg.cfl == cfl &&
+                    (!bc || std::equal(bc, bc + 6, h->cfg.bc));
+  if (same) return MHDGB_OK;
+  h->cfg.gam = gam;
+  h->cfg.cfl = cfl;
+  if (bc) std::copy(bc, bc + 6, h->cfg.bc);
+  h->prepared = false;
+  h->p64_valid = h->p_user;
+  destroy_graph(h);
+  return upload_desc(h);
+}
+
 int mhdgb_set_grid(mhdgb_solver* h, const double* x1a, const double* x2a, const double* x3a) {
   if (!h || !x1a || !x2a || !x3a) return MHDGB_ERR_ARG;
   int rc = set_device(h);

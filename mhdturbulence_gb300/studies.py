@@ -1,0 +1,183 @@
+"""Accuracy and throughput studies of the mixed and FP64 forms (GPU).
+
+    python -m mhdturbulence_gb300.studies turbulence [--n 256 --steps 200]
+    python -m mhdturbulence_gb300.studies kh_growth  [--n 128 --tmax 6]
+    python -m mhdturbulence_gb300.studies ensemble   [--members 64 --steps 20]
+    python -m mhdturbulence_gb300.studies all
+
+Each prints one JSON object per study.
+  turbulence: decaying turbulence (log-normal density, k^-2 velocity and vector-potential spectra,
+    <B_x> = 0.2, beta ~ 10) on a periodic n^3 cube, `steps` steps in both forms; errors of the mixed
+    form against FP64 (density L1/Linf, energy, div B) and conservation of mass and energy.
+  kh_growth: the KH layer to tmax in both forms with sqrt(<v_y^2>) sampled along the way; growth
+    rate Gamma fitted over 1 < t < tmax; also the low-beta variant (B_x = 1, p = 0.1).
+  ensemble: the seeded uneven 64-grid KH ensemble in both forms; aggregate Gcell-updates/s next to a
+    single 512^3 grid and the per-grid error of the mixed form against FP64.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+from . import ic
+from .ensemble import Ensemble, kh_ensemble_specs
+from .solver import Solver
+
+GAM = 5.0 / 3.0
+
+
+def _divb_rms(P, axes):
+    x1a, x2a, x3a = axes
+    n3, n2, _, n1 = P.shape
+    dx = np.diff(x1a)[2:2 + n1]
+    dy = np.diff(x2a)[2:2 + n2]
+    dz = np.diff(x3a)[2:2 + n3]
+    bx, by, bz = P[:, :, ic.NBM1, :], P[:, :, ic.NBM2, :], P[:, :, ic.NBM3, :]
+    d = (np.roll(bx, -1, 2) - np.roll(bx, 1, 2)) / (2 * dx[None, None, :]) \
+        + (np.roll(by, -1, 1) - np.roll(by, 1, 1)) / (2 * dy[None, :, None]) \
+        + (np.roll(bz, -1, 0) - np.roll(bz, 1, 0)) / (2 * dz[:, None, None])
+    return float(np.sqrt(np.mean(d ** 2)))
+
+
+def turbulence(n=256, steps=200, seed=7):
+    U0 = ic.prim_to_cons(ic.turbulence_prim(n, seed=seed), GAM)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with Solver(n, n, n, domain=ic.CUBE_DOMAIN, bc=ic.PERIODIC_BC, precision=prec) as s:
+            s.upload_cons(U0)
+            divb0 = _divb_rms(ic.interior(s.download_prim()), s.grid())
+            s.autotune(steps=2)
+            t0 = time.perf_counter()
+            s.step(steps)
+            r = s.sync()
+            wall = time.perf_counter() - t0
+            U = ic.interior(s.download_cons())
+            P = ic.interior(s.download_prim())
+            out[prec] = dict(r=r, U=U, P=P, divb0=divb0, divb=_divb_rms(P, s.grid()), wall=wall)
+    d, m = out["fp64"], out["mixed"]
+    U0i = ic.interior(U0)
+    rho_d, rho_m = d["U"][:, :, 0, :], m["U"][:, :, 0, :]
+    res = {
+        "study": "turbulence", "n": n, "steps": steps, "time_fp64": d["r"].time, "time_mixed": m["r"].time,
+        "rho_l1_rel": float(np.abs(rho_m - rho_d).sum() / np.abs(rho_d).sum()),
+        "rho_linf_rel": float(np.abs(rho_m - rho_d).max() / np.abs(rho_d).max()),
+        "energy_l1_rel": float(np.abs(m["U"][:, :, 4, :] - d["U"][:, :, 4, :]).sum() / np.abs(d["U"][:, :, 4, :]).sum()),
+        "divB_rms_initial": d["divb0"], "divB_rms_fp64": d["divb"], "divB_rms_mixed": m["divb"],
+        "mass_drift_fp64": float(abs(d["U"][:, :, 0, :].sum() / U0i[:, :, 0, :].sum() - 1)),
+        "mass_drift_mixed": float(abs(m["U"][:, :, 0, :].sum() / U0i[:, :, 0, :].sum() - 1)),
+        "energy_drift_fp64": float(abs(d["U"][:, :, 4, :].sum() / U0i[:, :, 4, :].sum() - 1)),
+        "energy_drift_mixed": float(abs(m["U"][:, :, 4, :].sum() / U0i[:, :, 4, :].sum() - 1)),
+        "wall_s_fp64": d["wall"], "wall_s_mixed": m["wall"],
+    }
+    return res
+
+
+def _kh_series(n, prec, tmax, sample_every, bx, p, vshear):
+    with Solver(n, n, n, precision=prec) as s:
+        U0 = ic.prim_to_cons(ic.kh_prim(n, n, n, seed=1, bx=bx, p=p, vshear=vshear), GAM)
+        s.upload_cons(U0)
+        s.set_stop(tmax, -1)
+        ts, vy = [0.0], [float(s.diag()[2])]
+        t0 = time.perf_counter()
+        while True:
+            s.step(sample_every)
+            r = s.sync()
+            d = s.diag()
+            ts.append(r.time)
+            vy.append(float(d[2]))
+            if r.done:
+                break
+        wall = time.perf_counter() - t0
+        U = ic.interior(s.download_cons())
+    return np.array(ts), np.array(vy), r, wall, U
+
+
+def _fit_growth(t, v, t0=1.0, t1=6.0):
+    sel = (t >= t0) & (t <= t1) & (v > 0)
+    if sel.sum() < 3:
+        return None
+    a, b = np.polyfit(t[sel], np.log(v[sel]), 1)
+    return float(a)
+
+
+def kh_growth(n=128, tmax=6.0, sample_every=200):
+    res = {"study": "kh_growth", "n": n, "tmax": tmax}
+    for name, bx, p in (("kh", 0.1, 1.0), ("low_beta", 1.0, 0.1)):
+        runs = {}
+        for prec in ("fp64", "mixed"):
+            runs[prec] = _kh_series(n, prec, tmax, sample_every, bx, p, 0.5)
+        (td, vd, rd, wd, Ud), (tm, vm, rm, wm, Um) = runs["fp64"], runs["mixed"]
+        gd, gm = _fit_growth(td, vd, 1.0, tmax), _fit_growth(tm, vm, 1.0, tmax)
+        vm_on_td = np.interp(td, tm, vm)
+        res[name] = {
+            "bx": bx, "p": p, "steps_fp64": rd.step, "steps_mixed": rm.step,
+            "gamma_fp64": gd, "gamma_mixed": gm,
+            "gamma_rel_diff": (abs(gm / gd - 1) if gd and gm else None),
+            "vy_rms_final_fp64": float(vd[-1]), "vy_rms_final_mixed": float(vm[-1]),
+            "vy_series_max_rel_diff": float(np.max(np.abs(vm_on_td - vd) / np.maximum(np.abs(vd), 1e-30))),
+            "rho_l1_rel_final": float(np.abs(Um[:, :, 0, :] - Ud[:, :, 0, :]).sum() / np.abs(Ud[:, :, 0, :]).sum()),
+            "wall_s_fp64": wd, "wall_s_mixed": wm,
+            "series_fp64": [[float(a), float(b)] for a, b in zip(td[::max(1, len(td) // 40)], vd[::max(1, len(td) // 40)])],
+        }
+    return res
+
+
+def ensemble(members=64, steps=20, err_steps=50, big=512, seed=2026):
+    specs = kh_ensemble_specs(members, seed=seed)
+    res = {"study": "ensemble", "members": members, "cells": int(sum(s["nx"] * s["ny"] * s["nz"] for s in specs))}
+    finals = {}
+    for prec, k in (("mixed", steps), ("fp64", max(2, steps // 8))):
+        with Ensemble(specs, precision=prec) as ens:
+            ens.init_kh()
+            best = ens.autotune(steps=2)
+            ens.time_steps(3)
+            ms = ens.time_steps(k)
+            res[f"{prec}_gcells"] = ens.cells * k / (ms * 1e-3) / 1e9
+            res[f"{prec}_tile_variant"] = best
+        with Ensemble(specs, precision=prec) as ens:
+            ens.init_kh()
+            ens.step(err_steps)
+            ens.sync()
+            finals[prec] = [ic.interior(m.download_cons()) for m in ens.members]
+        with Solver(big, big, big, precision=prec) as s:
+            s.init_kh(seed=1)
+            s.autotune(steps=2)
+            s.time_steps(2)
+            kk = 5 if prec == "mixed" else 2
+            ms = s.time_steps(kk)
+            res[f"{prec}_single_{big}_gcells"] = big ** 3 * kk / (ms * 1e-3) / 1e9
+        res[f"{prec}_ratio_vs_single"] = res[f"{prec}_gcells"] / res[f"{prec}_single_{big}_gcells"]
+    errs = []
+    for a, b in zip(finals["mixed"], finals["fp64"]):
+        errs.append(float(np.abs(a[:, :, 0, :] - b[:, :, 0, :]).sum() / np.abs(b[:, :, 0, :]).sum()))
+    res["per_member_rho_l1_rel"] = {"steps": err_steps, "max": max(errs), "median": float(np.median(errs)),
+                                    "min": min(errs)}
+    return res
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("study", choices=["turbulence", "kh_growth", "ensemble", "all"])
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--tmax", type=float, default=6.0)
+    ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--big", type=int, default=512)
+    a = ap.parse_args(argv)
+    todo = ["turbulence", "kh_growth", "ensemble"] if a.study == "all" else [a.study]
+    for st in todo:
+        if st == "turbulence":
+            r = turbulence(n=a.n or 256, steps=a.steps or 200)
+        elif st == "kh_growth":
+            r = kh_growth(n=a.n or 128, tmax=a.tmax)
+        else:
+            r = ensemble(members=a.members, steps=a.steps or 20, big=a.big)
+        print(json.dumps(r), flush=True)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
