@@ -108,6 +108,14 @@ int mhdgb_download_cons(mhdgb_solver* h, double* U);
 int mhdgb_download_prim(mhdgb_solver* h, double* P);
 int mhdgb_download_flux(mhdgb_solver* h, int dir, double* F);
 
+/* One variable at a time, for callers that keep one (itot, jtot, ktot) array per variable with i
+ * fastest, as the Fortran variants do (src_f90_acc_device/mhd.f90:29-36: d, mv1..3, et, b1..3, bp,
+ * Xcomp).  m is the reference's index: 0..9 for U (mden..mst), 0..11 for P (nden..nst). */
+int mhdgb_upload_cons_field(mhdgb_solver* h, int m, const double* a);
+int mhdgb_download_cons_field(mhdgb_solver* h, int m, double* a);
+int mhdgb_upload_prim_field(mhdgb_solver* h, int n, const double* a);
+int mhdgb_download_prim_field(mhdgb_solver* h, int n, double* a);
+
 /* ---- stage entry points (synchronous, FP64, reference rounding) ---- */
 /* ControlTimestep (mhd.cpp:1511-1561): dt = cfl * min over the interior; sets the handle's dt. */
 int mhdgb_control_timestep(mhdgb_solver* h, double* dt);
@@ -165,6 +173,11 @@ int mhdgb_autotune(mhdgb_solver* h, int steps, int* best);
 /* Measured FP64 FMA throughput of a device (GFLOP/s, 2 flops per FMA): the denominator of the
  * FP64-pipe roofline of the FP64 form, which is bound by FP64 issue rather than by HBM. */
 int mhdgb_measure_fp64_rate(int device, double* gflops);
+
+/* Self-test of the FP64 division used by the FMA-contracted FP64 form (FP32-seeded reciprocal with
+ * two Newton-Raphson steps) against IEEE division on n random operand pairs; *max_ulp receives
+ * the largest difference in units in the last place. */
+int mhdgb_selftest_division(int device, int n, unsigned long long seed, double* max_ulp);
 
 /* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):
  * out = {volume, <X(1-X)>, sqrt(<v_y^2>)} over the interior, FP64 sums. */

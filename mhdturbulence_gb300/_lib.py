@@ -50,6 +50,10 @@ SIGNATURES = {
     "mhdgb_download_cons": (C.c_int, [_vp, _dp]),
     "mhdgb_download_prim": (C.c_int, [_vp, _dp]),
     "mhdgb_download_flux": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_upload_cons_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_download_cons_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_upload_prim_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_download_prim_field": (C.c_int, [_vp, C.c_int, _dp]),
     "mhdgb_control_timestep": (C.c_int, [_vp, _dp]),
     "mhdgb_set_boundary": (C.c_int, [_vp]),
     "mhdgb_evaluate_ch": (C.c_int, [_vp, _dp]),
@@ -73,6 +77,7 @@ SIGNATURES = {
     "mhdgb_select_variant": (C.c_int, [_vp, C.c_int]),
     "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mhdgb_measure_fp64_rate": (C.c_int, [C.c_int, _dp]),
+    "mhdgb_selftest_division": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, _dp]),
     "mhdgb_diag": (C.c_int, [_vp, _dp]),
     "mhdgb_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double]),

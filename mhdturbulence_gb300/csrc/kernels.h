@@ -38,6 +38,7 @@ int variants_mixed(const FusedVariant** out);
 cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
 cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
 cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
+cudaError_t fdiv_selftest(int n, unsigned long long seed, unsigned long long* d_max_ulp, cudaStream_t s);
 }  // namespace detail
 
 }  // namespace mhdgb

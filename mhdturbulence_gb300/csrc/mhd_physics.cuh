@@ -15,9 +15,46 @@
 #ifndef MHDGB_VNS
 #error "define MHDGB_VNS (v_exact or v_fast) before including mhd_physics.cuh"
 #endif
+#ifndef MHDGB_FAST
+#error "define MHDGB_FAST (0: the reference's expressions, 1: shortened arithmetic) before including"
+#endif
+
+#include <type_traits>
+
+#include "common.cuh"
 
 namespace mhdgb {
 namespace MHDGB_VNS {
+
+// kFast selects, for the FMA-contracted builds, algebraically identical but shorter forms of a few
+// expressions (each marked below) and the division of fdiv(); the bit-exact build keeps the
+// reference's expressions and IEEE division.
+constexpr bool kFast = MHDGB_FAST != 0;
+
+// FP64 reciprocal from an FP32 seed (integer-pipe narrowing, the MUFU approximate reciprocal) and two
+// Newton-Raphson steps r <- r + r(1 - b r): the error of the seed (~2^-22) squares at each step,
+// so the result is within about one ulp of 1/b.
+__device__ __forceinline__ double rcp_newton(double b) {
+  float sf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(d2f_rne(b)));
+  double r = f2d_exact(sf);
+  r = fma(r, fma(-b, r, 1.0), r);
+  r = fma(r, fma(-b, r, 1.0), r);
+  return r;
+}
+
+// a / b: IEEE division in the exact build and in FP32; a * rcp_newton(b) in the FP64 fast build
+// (within ~1.5 ulp), with IEEE division where |b| is outside the FP32 seed's range.
+template <class R>
+__device__ __forceinline__ R fdiv(R a, R b) {
+  if constexpr (kFast && std::is_same<R, double>::value) {
+    const unsigned e = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
+    if (e < 1023u - 120u || e > 1023u + 120u) return a / b;
+    return a * rcp_newton(b);
+  } else {
+    return a / b;
+  }
+}
 
 // vanLeer, src_cpp_kokkos_host/mhd.cpp:89-95.  The limited slope of a cell c is
 // van_leer(P[c+1]-P[c], P[c]-P[c-1]); the reference evaluates the same expression for the left
@@ -25,7 +62,7 @@ namespace MHDGB_VNS {
 // per cell and direction gives both.
 template <class R>
 __device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
-  return (dsvp * dsvm > R(0)) ? R(2) * dsvp * dsvm / (dsvp + dsvm) : R(0);
+  return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
 }
 
 // Rotation maps of Prim2Cons1/2/3, mhd.cpp:1078-1118.
@@ -60,7 +97,7 @@ template <class R, int DIR>
 __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
   using D = Dir<DIR>;
   const R rho = Prim[nden];
-  const R rhoinv = R(1) / rho;
+  const R rhoinv = fdiv(R(1), rho);
   const R vsq = Prim[nve1] * Prim[nve1] + Prim[nve2] * Prim[nve2] + Prim[nve3] * Prim[nve3];
   const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
   Cons[mudn] = rho;
@@ -94,20 +131,24 @@ __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC
 
 // HLLD, mhd.cpp:97-417.  Writes the 10 rotated fluxes (slot mubp is left undefined: the GLM pair
 // replaces it).
-template <class R>
-__device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], R (&nflux)[NCONS]) {
+// Fast forms: the velocities m/rho of the rotated states are the reconstructed primitive
+// velocities themselves (Cons[muv?] = rho * Prim[nve?]), and rho*X/rho is X.
+template <class R, int DIR>
+__device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], const R (&Pl)[NPRIM],
+                                     const R (&Pr)[NPRIM], R (&nflux)[NCONS]) {
+  using D = Dir<DIR>;
   const R eps = R(1.0e-30);
   const R rol = leftst[mudn], eel = leftst[muet];
   const R rxl = leftst[muvu], ryl = leftst[muvv], rzl = leftst[muvw];
-  const R vxl = leftst[muvu] / leftst[mudn];
-  const R vyl = leftst[muvv] / leftst[mudn];
-  const R vzl = leftst[muvw] / leftst[mudn];
+  const R vxl = kFast ? Pl[D::nved] : leftst[muvu] / leftst[mudn];
+  const R vyl = kFast ? Pl[D::nvef] : leftst[muvv] / leftst[mudn];
+  const R vzl = kFast ? Pl[D::nveb] : leftst[muvw] / leftst[mudn];
   const R byl = leftst[mubv], bzl = leftst[mubw], ptl = leftst[mpre], scl = leftst[must];
   const R ror = rigtst[mudn], eer = rigtst[muet];
   const R rxr = rigtst[muvu], ryr = rigtst[muvv], rzr = rigtst[muvw];
-  const R vxr = rigtst[muvu] / rigtst[mudn];
-  const R vyr = rigtst[muvv] / rigtst[mudn];
-  const R vzr = rigtst[muvw] / rigtst[mudn];
+  const R vxr = kFast ? Pr[D::nved] : rigtst[muvu] / rigtst[mudn];
+  const R vyr = kFast ? Pr[D::nvef] : rigtst[muvv] / rigtst[mudn];
+  const R vzr = kFast ? Pr[D::nveb] : rigtst[muvw] / rigtst[mudn];
   const R byr = rigtst[mubv], bzr = rigtst[mubw], ptr = rigtst[mpre], scr = rigtst[must];
 
   // Step 1 (mhd.cpp:212-216)
@@ -124,12 +165,12 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   const R sdr = smax(R(1e-20), sr - vxr);
   const R rosdl = rol * sdl;
   const R rosdr = ror * sdr;
-  R temp = R(1) / (rosdr - rosdl);
+  R temp = fdiv(R(1), rosdr - rosdl);
   const R sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * temp;
   const R sdml = smin(R(-1e-20), sl - sm);
-  const R isdml = R(1) / sdml;
+  const R isdml = fdiv(R(1), sdml);
   const R sdmr = smax(R(1e-20), sr - sm);
-  const R isdmr = R(1) / sdmr;
+  const R isdmr = fdiv(R(1), sdmr);
   // Step 5 (mhd.cpp:264)
   const R ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * temp;
   // Step 5A (mhd.cpp:269-300)
@@ -139,10 +180,10 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   R sign1 = copysign(R(1), fabs(temp_fst) - eps);
   R maxs1 = smax(R(0), sign1);
   R mins1 = smin(R(0), sign1);
-  R itf = R(1) / (temp_fst + mins1);
+  R itf = fdiv(R(1), temp_fst + mins1);
   temp = bxs * (sdl - sdml) * itf;
   const R rolst = maxs1 * (rosdl * isdml) - mins1 * rol;
-  const R sclst = rolst / rol * scl;
+  const R sclst = kFast ? rolst * Pl[nst] : rolst / rol * scl;
   const R vxlst = maxs1 * sm - mins1 * vxl;
   const R rxlst = rolst * vxlst;
   const R vylst = maxs1 * (vyl - byl * temp) - mins1 * vyl;
@@ -161,10 +202,10 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   sign1 = copysign(R(1), fabs(temp_fst) - eps);
   maxs1 = smax(R(0), sign1);
   mins1 = smin(R(0), sign1);
-  itf = R(1) / (temp_fst + mins1);
+  itf = fdiv(R(1), temp_fst + mins1);
   temp = bxs * (sdr - sdmr) * itf;
   const R rorst = maxs1 * (rosdr * isdmr) - mins1 * ror;
-  const R scrst = rorst / ror * scr;
+  const R scrst = kFast ? rorst * Pr[nst] : rorst / ror * scr;
   const R vxrst = maxs1 * sm - mins1 * vxr;
   const R rxrst = rorst * vxrst;
   const R vyrst = maxs1 * (vyr - byr * temp) - mins1 * vyr;
@@ -186,7 +227,7 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   sign1 = copysign(R(1), abbx - eps);
   maxs1 = smax(R(0), sign1);
   mins1 = -smin(R(0), sign1);
-  const R invsumro = maxs1 / (sqrtrol + sqrtror);
+  const R invsumro = fdiv(maxs1, sqrtrol + sqrtror);
   temp = invsumro * (sqrtrol * vylst + sqrtror * vyrst + signbx * (byrst - bylst));
   const R vyldst = vylst * mins1 + temp;
   const R ryldst = rylst * mins1 + rolst * temp;
@@ -205,8 +246,8 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   const R eeldst = eelst - sqrtrol * signbx * (vdbstl - temp) * maxs1;
   const R eerdst = eerst + sqrtror * signbx * (vdbstr - temp) * maxs1;
   // Step 6 (mhd.cpp:381-415)
-  const R slst = (sm - abbx / sqrtrol) * maxs1;
-  const R srst = (sm + abbx / sqrtror) * maxs1;
+  const R slst = (sm - fdiv(abbx, sqrtrol)) * maxs1;
+  const R srst = (sm + fdiv(abbx, sqrtror)) * maxs1;
   sign1 = copysign(R(1), sm);
   maxs1 = smax(R(0), sign1);
   mins1 = -smin(R(0), sign1);
@@ -240,7 +281,7 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
   prim2cons<R, DIR>(Pl, Cl);
   prim2cons<R, DIR>(Pr, Cr);
-  hlld<R>(Cl, Cr, nf);
+  hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
   F[mden] = nf[mden];
   F[mrv1] = nf[D::orv1];
   F[mrv2] = nf[D::orv2];
@@ -250,7 +291,7 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
   F[D::ob_a] = nf[D::sb_a];
   F[D::ob_b] = nf[D::sb_b];
   F[D::glm] = R(0.5) * (Cl[mubp] + Cr[mubp]) - R(0.5) * chg * (Cr[mubu] - Cl[mubu]);
-  F[mbps] = (R(0.5) * (Cl[mubu] + Cr[mubu]) - R(0.5) / chg * (Cr[mubp] - Cl[mubp])) * chg * chg;
+  F[mbps] = (R(0.5) * (Cl[mubu] + Cr[mubu]) - fdiv(R(0.5), chg) * (Cr[mubp] - Cl[mubp])) * chg * chg;
   F[mst] = nf[mst];
 }
 
@@ -263,14 +304,14 @@ template <class R> __device__ __forceinline__ R right_state(R p, R s) { return p
 template <class R>
 __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPRIM]) {
   const R rho = u[mden];
-  const R rhoinv = R(1) / rho;
+  const R rhoinv = fdiv(R(1), rho);
   p[nden] = rho;
   p[nve1] = u[mrv1] * rhoinv;
   p[nve2] = u[mrv2] * rhoinv;
   p[nve3] = u[mrv3] * rhoinv;
   const R ekin = R(0.5) * (u[mrv1] * u[mrv1] + u[mrv2] * u[mrv2] + u[mrv3] * u[mrv3]) * rhoinv;
   const R emag = R(0.5) * (u[mbm1] * u[mbm1] + u[mbm2] * u[mbm2] + u[mbm3] * u[mbm3]);
-  p[nene] = (u[meto] - ekin - emag) / u[mden];
+  p[nene] = kFast ? (u[meto] - ekin - emag) * rhoinv : (u[meto] - ekin - emag) / u[mden];
   p[npre] = p[nene] * p[nden] * (gam - R(1));
   p[ncsp] = sqrt(p[nene] * gam * (gam - R(1)));
   p[nbm1] = u[mbm1];
@@ -283,10 +324,10 @@ __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPR
 // Per-cell CFL time (ControlTimestep, mhd.cpp:1542-1550): min over d of dx_d/(|v_d| + ctot).
 template <class R>
 __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
-  const R ctot = sqrt(p[ncsp] * p[ncsp] + (p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3]) / p[nden]);
-  R dt = dx / (fabs(p[nve1]) + ctot);
-  const R b = dy / (fabs(p[nve2]) + ctot);
-  const R c = dz / (fabs(p[nve3]) + ctot);
+  const R ctot = sqrt(p[ncsp] * p[ncsp] + fdiv(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
+  R dt = fdiv(dx, fabs(p[nve1]) + ctot);
+  const R b = fdiv(dy, fabs(p[nve2]) + ctot);
+  const R c = fdiv(dz, fabs(p[nve3]) + ctot);
   if (b < dt) dt = b;
   if (c < dt) dt = c;
   return dt;
@@ -296,9 +337,10 @@ __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
 template <class R>
 __device__ __forceinline__ R cell_ch(const R (&p)[NPRIM]) {
   const R css = p[ncsp] * p[ncsp];
-  const R ca1 = p[nbm1] * p[nbm1] / p[nden];
-  const R ca2 = p[nbm2] * p[nbm2] / p[nden];
-  const R ca3 = p[nbm3] * p[nbm3] / p[nden];
+  const R ri = kFast ? fdiv(R(1), p[nden]) : R(0);  // fast form: one reciprocal of rho
+  const R ca1 = kFast ? p[nbm1] * p[nbm1] * ri : p[nbm1] * p[nbm1] / p[nden];
+  const R ca2 = kFast ? p[nbm2] * p[nbm2] * ri : p[nbm2] * p[nbm2] / p[nden];
+  const R ca3 = kFast ? p[nbm3] * p[nbm3] * ri : p[nbm3] * p[nbm3] / p[nden];
   const R cts = css + ca1 + ca2 + ca3;
   const R cm1 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca1)) / R(2));
   const R ch1 = (fabs(p[nve1]) + cm1);

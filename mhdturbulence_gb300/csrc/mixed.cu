@@ -2,6 +2,7 @@
 // (-prec-div=false -prec-sqrt=false -ftz=true): those only touch the FP32 reconstruction and Riemann
 // solve; the FP64 state update and pressure recovery are unaffected, and the compensated sums use
 // explicitly rounded intrinsics.
+#define MHDGB_FAST 1
 #define MHDGB_VNS v_mixed
 #include "fused.cuh"
 #include "kernels.h"

@@ -75,6 +75,18 @@ __global__ void k_ctrl_set_stop(Ctrl* c, double tmax, unsigned long long max_ste
   c->done = (c->time > tmax || c->step >= max_step) ? 1u : 0u;
 }
 
+// One variable between a dense (k, j, i) host array and its rows in the (k, j, n, i) device layout.
+__global__ void k_field(const double* __restrict__ src, double* __restrict__ dst, int itot, int ip, int nv, int n,
+                        size_t rows, int to_device) {
+  const size_t tot = rows * (size_t)itot;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / itot, i = t % itot;  // r = j + jtot*k
+    const size_t d = (r * nv + n) * ip + i;
+    if (to_device) dst[d] = src[t];
+    else dst[t] = src[d];
+  }
+}
+
 // Row repack between the dense host layout (row length itot) and the padded device pitch ip.
 __global__ void k_repack(const double* __restrict__ src, double* __restrict__ dst, int itot, int ip, size_t rows,
                          int to_pitched) {
@@ -706,6 +718,45 @@ int mhdgb_download_prim(mhdgb_solver* h, double* P) {
   return MHDGB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+int field_transfer(mhdgb_solver* h, bool cons, int n, const double* in, double* out) {
+  const int nv = cons ? NCONS : NPRIM;
+  if (!h || n < 0 || n >= nv || (!in && !out)) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = settle(h))) return rc;
+  if (!cons && (rc = ensure_stage_bufs(h))) return rc;
+  const Layout& L = h->L;
+  const size_t rows = (size_t)L.jtot * L.ktot, bytes = rows * L.itot * sizeof(double);
+  double* st = staging(h);
+  if (!st) return fail(h, MHDGB_ERR_NOMEM, "staging buffer");
+  double* arr = cons ? h->U : h->P64[cur_index(h)];
+  if (in) {
+    if (!cons && !h->p64_valid && (rc = ensure_p64(h))) return rc;  // keep the other fields consistent
+    CK(h, cudaMemcpyAsync(st, in, bytes, cudaMemcpyHostToDevice, h->stream));
+    k_field<<<h->nsm * 8, 256, 0, h->stream>>>(st, arr, L.itot, L.ip, nv, n, rows, 1);
+    CK(h, cudaGetLastError());
+    if (cons) { h->have_state = true; h->prepared = false; h->p64_valid = h->p_user; }
+    else { h->p64_valid = true; h->p_user = true; h->prepared = false; }
+  } else {
+    if (!cons && (rc = ensure_p64(h))) return rc;
+    k_field<<<h->nsm * 8, 256, 0, h->stream>>>(arr, st, L.itot, L.ip, nv, n, rows, 0);
+    CK(h, cudaGetLastError());
+    CK(h, cudaMemcpyAsync(out, st, bytes, cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mhdgb_upload_cons_field(mhdgb_solver* h, int m, const double* a) { return field_transfer(h, true, m, a, nullptr); }
+int mhdgb_download_cons_field(mhdgb_solver* h, int m, double* a) { return field_transfer(h, true, m, nullptr, a); }
+int mhdgb_upload_prim_field(mhdgb_solver* h, int n, const double* a) { return field_transfer(h, false, n, a, nullptr); }
+int mhdgb_download_prim_field(mhdgb_solver* h, int n, double* a) { return field_transfer(h, false, n, nullptr, a); }
+
 int mhdgb_download_flux(mhdgb_solver* h, int dir, double* F) {
   if (!h || !F || dir < 1 || dir > 3) return MHDGB_ERR_ARG;
   int rc = set_device(h);
@@ -983,6 +1034,21 @@ int mhdgb_measure_fp64_rate(int device, double* gflops) {
   cudaFree(out);
   if (e != cudaSuccess) return MHDGB_ERR_CUDA;
   *gflops = 2.0 * 8.0 * iters * (double)grid * bs / (best * 1e-3) / 1e9;  // 2 flops per FMA
+  return MHDGB_OK;
+}
+
+int mhdgb_selftest_division(int device, int n, unsigned long long seed, double* max_ulp) {
+  if (!max_ulp || n < 1) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return MHDGB_ERR_NOMEM;
+  unsigned long long h = 0;
+  cudaError_t e = cudaMemset(d, 0, sizeof(*d));
+  if (e == cudaSuccess) e = detail::fdiv_selftest(n, seed, d, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return MHDGB_ERR_CUDA;
+  *max_ulp = (double)h;
   return MHDGB_OK;
 }
 

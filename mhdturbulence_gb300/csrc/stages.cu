@@ -8,6 +8,7 @@
 //   UpdatePrimitvP     (mhd.cpp:1447-1509)   -> k_update_prim
 //   ControlTimestep / EvaluateCh (mhd.cpp:1511-1611, + MPIminfind/MPImaxfind) -> k_reduce_dt_ch
 //   SetBoundaryCondition (boundary.cpp:750-893, single-rank SendRecvBoundary) -> k_pack + k_unpack
+#define MHDGB_FAST 0
 #define MHDGB_VNS v_exact
 #include "fused.cuh"
 #include "kernels.h"

@@ -10,7 +10,8 @@ Each prints one JSON object per study.
     <B_x> = 0.2, beta ~ 10) on a periodic n^3 cube, `steps` steps in both forms; errors of the mixed
     form against FP64 (density L1/Linf, energy, div B) and conservation of mass and energy.
   kh_growth: the KH layer to tmax in both forms with sqrt(<v_y^2>) sampled along the way; growth
-    rate Gamma fitted over 1 < t < tmax; also the low-beta variant (B_x = 1, p = 0.1).
+    rate Gamma fitted over the exponential phase 1 < t < 4 (the layer saturates near t = 4.5 at
+    these resolutions); also the low-beta variant (B_x = 1, p = 0.1) over its stable window.
   ensemble: the seeded uneven 64-grid KH ensemble in both forms; aggregate Gcell-updates/s next to a
     single 512^3 grid and the per-grid error of the mixed form against FP64.
 """
@@ -24,6 +25,7 @@ import time
 import numpy as np
 
 from . import ic
+from ._lib import MhdgbError
 from .ensemble import Ensemble, kh_ensemble_specs
 from .solver import Solver
 
@@ -76,11 +78,11 @@ def turbulence(n=256, steps=200, seed=7):
     return res
 
 
-def _kh_series(n, prec, tmax, sample_every, bx, p, vshear):
+def _kh_series(n, prec, tmax, sample_every, bx, p, vshear, max_steps=-1):
     with Solver(n, n, n, precision=prec) as s:
         U0 = ic.prim_to_cons(ic.kh_prim(n, n, n, seed=1, bx=bx, p=p, vshear=vshear), GAM)
         s.upload_cons(U0)
-        s.set_stop(tmax, -1)
+        s.set_stop(tmax, max_steps)
         ts, vy = [0.0], [float(s.diag()[2])]
         t0 = time.perf_counter()
         while True:
@@ -93,7 +95,8 @@ def _kh_series(n, prec, tmax, sample_every, bx, p, vshear):
                 break
         wall = time.perf_counter() - t0
         U = ic.interior(s.download_cons())
-    return np.array(ts), np.array(vy), r, wall, U
+        P = ic.interior(s.download_prim())
+    return np.array(ts), np.array(vy), r, wall, U, P
 
 
 def _fit_growth(t, v, t0=1.0, t1=6.0):
@@ -104,25 +107,52 @@ def _fit_growth(t, v, t0=1.0, t1=6.0):
     return float(a)
 
 
-def kh_growth(n=128, tmax=6.0, sample_every=200):
+def _first_bad_step(n, bx, p, limit):
+    """Number of FP64 steps the low-beta state survives before the status word reports a
+    non-finite or non-positive cell (the reference scheme has no positivity fix)."""
+    with Solver(n, n, n, precision="fp64") as s:
+        s.upload_cons(ic.prim_to_cons(ic.kh_prim(n, n, n, seed=1, bx=bx, p=p), GAM))
+        for k in range(1, limit + 1):
+            s.step(1)
+            try:
+                s.sync()
+            except MhdgbError:
+                return k
+    return None
+
+
+def kh_growth(n=128, tmax=6.0, sample_every=200, low_beta_steps=None):
+    """KH growth in both forms.  The low-beta variant (B_x = 1, p = 0.1) loses pressure positivity
+    under the reference scheme within a few hundred steps (the oracle does too), so it is compared
+    over its first `low_beta_steps` steps, where the FP64 pressure recovery matters most."""
     res = {"study": "kh_growth", "n": n, "tmax": tmax}
-    for name, bx, p in (("kh", 0.1, 1.0), ("low_beta", 1.0, 0.1)):
+    bad = _first_bad_step(n, 1.0, 0.1, 400)
+    if low_beta_steps is None:
+        low_beta_steps = max(1, (bad - 1) * 3 // 4) if bad else 100
+    res["low_beta_first_failing_step_fp64"] = bad
+    for name, bx, p, steps in (("kh", 0.1, 1.0, -1), ("low_beta", 1.0, 0.1, low_beta_steps)):
         runs = {}
         for prec in ("fp64", "mixed"):
-            runs[prec] = _kh_series(n, prec, tmax, sample_every, bx, p, 0.5)
-        (td, vd, rd, wd, Ud), (tm, vm, rm, wm, Um) = runs["fp64"], runs["mixed"]
-        gd, gm = _fit_growth(td, vd, 1.0, tmax), _fit_growth(tm, vm, 1.0, tmax)
+            every = sample_every if steps < 0 else max(1, steps // 10)
+            runs[prec] = _kh_series(n, prec, tmax, every, bx, p, 0.5, max_steps=steps)
+        (td, vd, rd, wd, Ud, Pd), (tm, vm, rm, wm, Um, Pm) = runs["fp64"], runs["mixed"]
         vm_on_td = np.interp(td, tm, vm)
-        res[name] = {
-            "bx": bx, "p": p, "steps_fp64": rd.step, "steps_mixed": rm.step,
-            "gamma_fp64": gd, "gamma_mixed": gm,
-            "gamma_rel_diff": (abs(gm / gd - 1) if gd and gm else None),
+        out = {
+            "bx": bx, "p": p, "steps_fp64": rd.step, "steps_mixed": rm.step, "t_end": float(td[-1]),
             "vy_rms_final_fp64": float(vd[-1]), "vy_rms_final_mixed": float(vm[-1]),
             "vy_series_max_rel_diff": float(np.max(np.abs(vm_on_td - vd) / np.maximum(np.abs(vd), 1e-30))),
             "rho_l1_rel_final": float(np.abs(Um[:, :, 0, :] - Ud[:, :, 0, :]).sum() / np.abs(Ud[:, :, 0, :]).sum()),
+            "p_linf_rel_final": float(np.abs(Pm[:, :, 5, :] - Pd[:, :, 5, :]).max() / np.abs(Pd[:, :, 5, :]).max()),
+            "p_l1_rel_final": float(np.abs(Pm[:, :, 5, :] - Pd[:, :, 5, :]).sum() / np.abs(Pd[:, :, 5, :]).sum()),
             "wall_s_fp64": wd, "wall_s_mixed": wm,
-            "series_fp64": [[float(a), float(b)] for a, b in zip(td[::max(1, len(td) // 40)], vd[::max(1, len(td) // 40)])],
         }
+        if steps < 0:
+            gd, gm = _fit_growth(td, vd, 1.0, min(tmax, 4.0)), _fit_growth(tm, vm, 1.0, min(tmax, 4.0))
+            out.update({"gamma_fit_window": [1.0, min(tmax, 4.0)], "gamma_fp64": gd, "gamma_mixed": gm,
+                        "gamma_rel_diff": (abs(gm / gd - 1) if gd and gm else None),
+                        "series_fp64": [[float(a), float(b)] for a, b in
+                                        zip(td[::max(1, len(td) // 40)], vd[::max(1, len(td) // 40)])]})
+        res[name] = out
     return res
 
 

@@ -305,3 +305,29 @@ def test_reference_style_upload_of_p_and_u():
         dt, chg = s.stage_step()
         assert dt == case.z["dts"][0] and chg == case.z["chgs"][0]
         assert np.array_equal(s.download_cons(), case.z["U1"])
+
+
+def test_fast_fp64_division_is_within_two_ulp():
+    import ctypes as C
+    from mhdturbulence_gb300 import _lib
+    m = C.c_double()
+    assert _lib.lib().mhdgb_selftest_division(0, 1 << 22, 12345, C.byref(m)) == 0
+    assert m.value <= 2.0, m.value
+
+
+def test_per_field_transfers_match_full_arrays():
+    nx, ny, nz = 10, 12, 8
+    rng = np.random.default_rng(3)
+    with Solver(nx, ny, nz) as s:
+        U = rng.standard_normal((s.ktot, s.jtot, 10, s.itot))
+        s.upload_cons(U)
+        import ctypes as C
+        L = s._L
+        for m in (0, 4, 9):
+            a = np.zeros((s.ktot, s.jtot, s.itot))
+            assert L.mhdgb_download_cons_field(s._h, m, a.ctypes.data_as(C.POINTER(C.c_double))) == 0
+            assert np.array_equal(a, U[:, :, m, :])
+        b = rng.standard_normal((s.ktot, s.jtot, s.itot))
+        assert L.mhdgb_upload_cons_field(s._h, 3, b.ctypes.data_as(C.POINTER(C.c_double))) == 0
+        U[:, :, 3, :] = b
+        assert np.array_equal(s.download_cons(), U)
