@@ -272,6 +272,122 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   nflux[mbps] = R(0);
 }
 
+// HLLD in branch form, for the FMA-contracted FP64 build.  Same states and fluxes as hlld(), but the selections
+// the reference performs with 0/1 masks (maxs1/mins1 of mhd.cpp:272-275, 306-308, 343-346, 384-386)
+// are branches: the degenerate-field forms are taken only when their conditions hold, and only the
+// upwind side of the final flux is formed.  Results agree with hlld() to rounding (and in the sign
+// of zero results).  On GB300 it cuts the FP64 step by about 16%; the FP32 reconstruction of the
+// mixed form is issue-latency bound rather than FP64-pipe bound and keeps the mask form, which
+// measured slightly faster there.
+template <class R, int DIR>
+__device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], const R (&Pl)[NPRIM],
+                                            const R (&Pr)[NPRIM], R (&nflux)[NCONS]) {
+  using D = Dir<DIR>;
+  const R eps = R(1.0e-30);
+  const R rol = leftst[mudn], eel = leftst[muet];
+  const R vxl = Pl[D::nved], vyl = Pl[D::nvef], vzl = Pl[D::nveb];
+  const R byl = leftst[mubv], bzl = leftst[mubw], ptl = leftst[mpre];
+  const R ror = rigtst[mudn], eer = rigtst[muet];
+  const R vxr = Pr[D::nved], vyr = Pr[D::nvef], vzr = Pr[D::nveb];
+  const R byr = rigtst[mubv], bzr = rigtst[mubw], ptr = rigtst[mpre];
+  const R cfl = leftst[mcsp], cfr = rigtst[mcsp];
+  const R cmax = smax(cfl, cfr);
+  const R sl = smin(vxl, vxr) - cmax;
+  const R sr = smax(vxl, vxr) + cmax;
+  const R sdl = smin(R(-1e-20), sl - vxl);
+  const R sdr = smax(R(1e-20), sr - vxr);
+  const R rosdl = rol * sdl;
+  const R rosdr = ror * sdr;
+  const R tden = fdiv(R(1), rosdr - rosdl);
+  const R sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * tden;
+  const R ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * tden;
+  const R bxs = R(0.5) * (leftst[mubu] + rigtst[mubu]);
+  const R bxsq = bxs * bxs;
+  const bool left = !signbit(sm);  // copysign(1, sm) > 0, mhd.cpp:384
+  // upwind side only: s = side speed, sd = s - v, sdm = s - sm, ro/e/v/b of that side
+  const R s_ = left ? sl : sr;
+  const R sd = left ? sdl : sdr;
+  const R rosd = left ? rosdl : rosdr;
+  const R sdm = left ? smin(R(-1e-20), sl - sm) : smax(R(1e-20), sr - sm);
+  const R ro = left ? rol : ror, ee = left ? eel : eer, pt = left ? ptl : ptr;
+  const R vx = left ? vxl : vxr, vy = left ? vyl : vyr, vz = left ? vzl : vzr;
+  const R by = left ? byl : byr, bz = left ? bzl : bzr;
+  const R sc = left ? Pl[nst] : Pr[nst];
+  // star state of the upwind side (Step 5A/5B)
+  R rost = ro, vxst = vx, vyst = vy, vzst = vz, byst = by, bzst = bz, eest = ee;
+  const R temp_fst = rosd * sdm - bxsq;
+  const R isdm = fdiv(R(1), sdm);
+  if (!(fabs(temp_fst) - eps < R(0))) {
+    const R itf = fdiv(R(1), temp_fst);
+    const R t1 = bxs * (sd - sdm) * itf;
+    rost = rosd * isdm;
+    vxst = sm;
+    vyst = vy - by * t1;
+    vzst = vz - bz * t1;
+    const R t2 = (rosd * sd - bxsq) * itf;
+    byst = by * t2;
+    bzst = bz * t2;
+    const R vdbst = vxst * bxs + vyst * byst + vzst * bzst;
+    eest = (sd * ee - pt * vx + ptst * sm + bxs * (vx * bxs + vy * by + vz * bz - vdbst)) * isdm;
+  }
+  // Alfven (double-star) correction of the tangential states and energy (Step 5C), needs both
+  // star states: the other side's star state is formed the same way.
+  const R so_sd = left ? sdr : sdl;
+  const R so_rosd = left ? rosdr : rosdl;
+  const R so_sdm = left ? smax(R(1e-20), sr - sm) : smin(R(-1e-20), sl - sm);
+  const R so_ro = left ? ror : rol;
+  const R so_vy = left ? vyr : vyl, so_vz = left ? vzr : vzl, so_by = left ? byr : byl, so_bz = left ? bzr : bzl;
+  R so_rost = so_ro, so_vyst = so_vy, so_vzst = so_vz, so_byst = so_by, so_bzst = so_bz;
+  const R so_tf = so_rosd * so_sdm - bxsq;
+  if (!(fabs(so_tf) - eps < R(0))) {
+    const R itf = fdiv(R(1), so_tf);
+    const R t1 = bxs * (so_sd - so_sdm) * itf;
+    so_rost = so_rosd * fdiv(R(1), so_sdm);
+    so_vyst = so_vy - so_by * t1;
+    so_vzst = so_vz - so_bz * t1;
+    const R t2 = (so_rosd * so_sd - bxsq) * itf;
+    so_byst = so_by * t2;
+    so_bzst = so_bz * t2;
+  }
+  const R abbx = fabs(bxs);
+  R vydst = vyst, vzdst = vzst, bydst = byst, bzdst = bzst, eedst = eest, sst = R(0);
+  if (!(abbx - eps < R(0))) {
+    const R signbx = copysign(R(1), bxs);
+    const R sq = sqrt(rost), so_sq = sqrt(so_rost);
+    // (sqrtrol, sqrtror) ordered as in the reference
+    const R sql = left ? sq : so_sq, sqr = left ? so_sq : sq;
+    const R invsumro = fdiv(R(1), sql + sqr);
+    const R vyl_st = left ? vyst : so_vyst, vyr_st = left ? so_vyst : vyst;
+    const R vzl_st = left ? vzst : so_vzst, vzr_st = left ? so_vzst : vzst;
+    const R byl_st = left ? byst : so_byst, byr_st = left ? so_byst : byst;
+    const R bzl_st = left ? bzst : so_bzst, bzr_st = left ? so_bzst : bzst;
+    vydst = invsumro * (sql * vyl_st + sqr * vyr_st + signbx * (byr_st - byl_st));
+    vzdst = invsumro * (sql * vzl_st + sqr * vzr_st + signbx * (bzr_st - bzl_st));
+    bydst = invsumro * (sql * byr_st + sqr * byl_st + signbx * sql * sqr * (vyr_st - vyl_st));
+    bzdst = invsumro * (sql * bzr_st + sqr * bzl_st + signbx * sql * sqr * (vzr_st - vzl_st));
+    const R vdbst = vxst * bxs + vyst * byst + vzst * bzst;
+    const R tdd = sm * bxs + vydst * bydst + vzdst * bzdst;
+    eedst = left ? eest - sq * signbx * (vdbst - tdd) : eest + sq * signbx * (vdbst - tdd);
+    sst = left ? sm - fdiv(abbx, sq) : sm + fdiv(abbx, sq);
+  }
+  // Step 6: flux of the upwind side
+  const R ms = left ? smin(s_, R(0)) : smax(s_, R(0));
+  const R msst = left ? smin(sst, R(0)) : smax(sst, R(0));
+  const R* cst = left ? leftst : rigtst;
+  const R rx = cst[muvu], ry = cst[muvv], rz = cst[muvw];
+  nflux[mden] = cst[mfdn] + (rost - ro) * ms;
+  nflux[meto] = cst[mfet] + (eest - ee) * ms + (eedst - eest) * msst;
+  nflux[mrv1] = cst[mfvu] + (rost * vxst - rx) * ms;
+  const R ryst = rost * vyst, rzst = rost * vzst;
+  nflux[mrv2] = cst[mfvv] + (ryst - ry) * ms + (rost * vydst - ryst) * msst;
+  nflux[mrv3] = cst[mfvw] + (rzst - rz) * ms + (rost * vzdst - rzst) * msst;
+  nflux[mbm1] = R(0);
+  nflux[mbm2] = cst[mfbv] + (byst - by) * ms + (bydst - byst) * msst;
+  nflux[mbm3] = cst[mfbw] + (bzst - bz) * ms + (bzdst - bzst) * msst;
+  nflux[mst] = cst[mfst] + (rost * sc - cst[must]) * ms;
+  nflux[mbps] = R(0);
+}
+
 // Face flux from the reconstructed left/right primitive states: Prim2Cons of both sides, HLLD,
 // then the rotation back to (rho, m1, m2, m3, E, B1, B2, B3, psi, X) order with the GLM pair for
 // the normal field and psi (mhd.cpp:1223-1240 and equivalents).
@@ -281,7 +397,8 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
   prim2cons<R, DIR>(Pl, Cl);
   prim2cons<R, DIR>(Pr, Cr);
-  hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
+  if constexpr (kFast && std::is_same<R, double>::value) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf);
+  else hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
   F[mden] = nf[mden];
   F[mrv1] = nf[D::orv1];
   F[mrv2] = nf[D::orv2];
