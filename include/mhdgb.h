@@ -212,6 +212,33 @@ int mhdgb_ensemble_variant(const mhdgb_ensemble* e);
 /* Times every compiled tile shape on the whole ensemble (states restored) and keeps the fastest. */
 int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best);
 
+/* ---- allocation-free ghost fill ----
+ * This entry point has no counterpart in the reference.  It performs SetBoundaryCondition
+ * (boundary.cpp:750-893, single-rank fills) -- the same values as mhdgb_set_boundary, bit for bit --
+ * on a primitive array that the caller owns, without a handle and without allocating device memory.
+ * It is meant for callers that cannot let a library allocate on their call path: device memory under
+ * a fixed budget or in the caller's own pool, or asynchronous work on other streams that the
+ * device-wide synchronisation of cudaMalloc / cudaFree would stall.
+ *
+ * P      device pointer (on the current device) to the 12 primitive fields, element (n,k,j,i) at
+ *        i + pitch*(n + 12*(j + (ny+5)*k)), i < nx+5 -- the reference's FieldArray layout when
+ *        pitch = nx+5; pitch = 0 means nx+5.
+ * nx..nz interior cells (each >= 2); bc: boundary_xin .. boundary_zout (MHDGB_BC_*).
+ * stream a cudaStream_t (NULL: the legacy default stream).  The call only enqueues two kernels and
+ *        returns; errors of the kernels themselves appear on that stream.
+ *
+ * Scratch: one fixed array of MHDGB_NOALLOC_SCRATCH_BYTES in the library's static device memory,
+ * of which a call uses 1536*(nx+ny+nz+7) bytes; calls with nx+ny+nz > MHDGB_NOALLOC_MAX_EXTENT_SUM
+ * return MHDGB_ERR_SCRATCH before touching the device.  No part of the scratch has to start at zero.
+ * The first call on each device resolves the scratch address (cudaGetSymbolAddress, which also loads
+ * the module): make that first call before any stream capture begins.  All calls on one device share
+ * the one scratch array, so calls that overlap in time -- on different streams, or from several host
+ * threads without ordering between their streams -- race on it and give wrong ghosts; order them. */
+#define MHDGB_ERR_SCRATCH (-8) /* request larger than a fixed scratch area */
+#define MHDGB_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define MHDGB_NOALLOC_MAX_EXTENT_SUM 2723
+int mhdgb_fill_ghosts_noalloc(double* P, int nx, int ny, int nz, int pitch, const int* bc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,8 @@ _lib = None
 MHDGB_FP64, MHDGB_FP64_EXACT, MHDGB_MIXED = 0, 1, 2
 PRECISIONS = {"fp64": MHDGB_FP64, "fp64_exact": MHDGB_FP64_EXACT, "mixed": MHDGB_MIXED}
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "non-positive rho/p",
-          -5: "device wait timed out", -6: "call out of order", -7: "device allocation failed"}
+          -5: "device wait timed out", -6: "call out of order", -7: "device allocation failed",
+          -8: "grid too large for the fixed scratch"}
 
 # every symbol include/mhdgb.h declares, with (restype, argtypes)
 _dp = C.POINTER(C.c_double)
@@ -56,6 +57,7 @@ SIGNATURES = {
     "mhdgb_download_prim_field": (C.c_int, [_vp, C.c_int, _dp]),
     "mhdgb_control_timestep": (C.c_int, [_vp, _dp]),
     "mhdgb_set_boundary": (C.c_int, [_vp]),
+    "mhdgb_fill_ghosts_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), _vp]),
     "mhdgb_evaluate_ch": (C.c_int, [_vp, _dp]),
     "mhdgb_flux": (C.c_int, [_vp, C.c_int]),
     "mhdgb_update_conserv": (C.c_int, [_vp]),

@@ -7,6 +7,7 @@ Translation units are compiled in parallel with nvcc:
   csrc/fp64.cu                  FP64 fused steps (FMA contraction), several tile shapes
   csrc/mixed.cu                 FP32-mixed fused steps (fast FP32 div/sqrt), several tile shapes
   csrc/solver.cu                host side of the C ABI (include/mhdgb.h)
+  csrc/ghost_noalloc.cu         allocation-free ghost fill on a caller-owned array
 and linked into mhdturbulence_gb300/_build/libmhdgb.so (static CUDA runtime).
 """
 from __future__ import annotations
@@ -33,6 +34,7 @@ UNITS = [
     ("fp64.cu", []),
     ("mixed.cu", ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("solver.cu", []),
+    ("ghost_noalloc.cu", []),
 ]
 
 

@@ -530,6 +530,7 @@ const char* mhdgb_status_string(int s) {
     case MHDGB_ERR_TIMEOUT: return "device-side wait timed out";
     case MHDGB_ERR_STATE: return "call out of order";
     case MHDGB_ERR_NOMEM: return "device allocation failed";
+    case MHDGB_ERR_SCRATCH: return "grid too large for the fixed scratch of mhdgb_fill_ghosts_noalloc";
     default: return "unknown status";
   }
 }
