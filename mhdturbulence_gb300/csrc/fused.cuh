@@ -241,8 +241,10 @@ __device__ __forceinline__ void update_cell(const DivAcc<float>& acc, const doub
   u[mbps] = u[mbps] * f2d_exact(1.0f - dtf * (0.1f * chf * imax));
 }
 
-template <class R, int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT, 1)
+// MINB: CTAs per SM the register allocation must allow (__launch_bounds__); 2 at 256 threads caps
+// a thread at 128 registers, which the FP32 form meets without spills.
+template <class R, int TX, int TY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc) {
   using S = FusedSmem<R, TX, TY, NT>;
   constexpr int NBUF = S::NBUF, PX = S::PX;
@@ -557,22 +559,22 @@ __global__ void k_recover(FusedArgs a, int which, RedSlot* slot) {
 }
 
 // Host side of one instantiation of the fused kernel.
-template <class R, int TX, int TY, int NT>
+template <class R, int TX, int TY, int NT, int MINB = 1>
 struct FusedLauncher {
   using S = FusedSmem<R, TX, TY, NT>;
-  static FusedShape shape() { return FusedShape{TX, TY, S::total, NT, (int)sizeof(R)}; }
+  static FusedShape shape() { return FusedShape{TX, TY, S::total, NT, (int)sizeof(R), MINB}; }
   static cudaError_t prepare() {
-    return cudaFuncSetAttribute(k_fused_step<R, TX, TY, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_fused_step<R, TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)S::total);
   }
   static int ctas_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_fused_step<R, TX, TY, NT>, NT, S::total) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_fused_step<R, TX, TY, NT, MINB>, NT, S::total) != cudaSuccess)
       return 0;
     return n;
   }
   static cudaError_t launch(const InstanceDesc* desc, LaunchCtrl* lc, int grid, cudaStream_t s) {
-    k_fused_step<R, TX, TY, NT><<<grid, NT, S::total, s>>>(desc, lc);
+    k_fused_step<R, TX, TY, NT, MINB><<<grid, NT, S::total, s>>>(desc, lc);
     return cudaGetLastError();
   }
   static FusedVariant variant(FusedKind kind) {

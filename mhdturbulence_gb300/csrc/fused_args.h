@@ -13,6 +13,7 @@ struct FusedShape {
   size_t smem;         // dynamic shared memory per CTA
   int threads;         // threads per CTA
   int elem;            // bytes per P element (8 or 4)
+  int min_ctas;        // CTAs per SM the kernel's register budget was compiled for
 };
 
 struct FusedArgs {

@@ -16,6 +16,8 @@ int variants_mixed(const FusedVariant** out) {
       v_mixed::FusedLauncher<float, 32, 8, 256>::variant(FUSED_MIXED),
       v_mixed::FusedLauncher<float, 16, 8, 128>::variant(FUSED_MIXED),
       v_mixed::FusedLauncher<float, 64, 4, 256>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncher<float, 32, 4, 256, 2>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncher<float, 16, 8, 256, 2>::variant(FUSED_MIXED),
   };
   *out = v;
   return (int)(sizeof(v) / sizeof(v[0]));
