@@ -35,6 +35,7 @@ extern "C" {
 #define MHDGB_ERR_TIMEOUT (-5)    /* a bounded device-side wait gave up */
 #define MHDGB_ERR_STATE (-6)      /* call out of order (e.g. no state uploaded) */
 #define MHDGB_ERR_NOMEM (-7)      /* device allocation failed */
+#define MHDGB_ERR_IO (-9)         /* a snapshot file could not be written */
 
 /* boundary types, src_cpp_kokkos_host/config.hpp:29-31 */
 #define MHDGB_BC_PERIODIC 1
@@ -96,6 +97,18 @@ size_t mhdgb_device_bytes(const mhdgb_solver* h);
 /* Change gam (hydflux_mod::gam), the CFL factor and the boundary types (boundary_mod::boundary_xin
  * ... _zout, boundary.cpp:26-31) of an existing handle; bc may be NULL to keep them. */
 int mhdgb_set_physics(mhdgb_solver* h, double gam, double cfl, const int* bc);
+
+/* Riemann solver of the face fluxes, for the stage path and every fused form: HLLD (the C++ path's,
+ * mhd.cpp:97-417; the default), or the Fortran variant's alternatives HLLE (src_f90_acc_device/
+ * mhd.f90:877-907) and HLLC (mhd.f90:909-1141), selectable there by editing the calls at
+ * mhd.f90:478-480, 665-667, 852-854.  The Fortran HLLC reads a passive-scalar star state it never
+ * sets; here it is the scalar scaled by the star-state density ratio, as that routine scales the
+ * transverse field. */
+#define MHDGB_RIEMANN_HLLD 0
+#define MHDGB_RIEMANN_HLLE 1
+#define MHDGB_RIEMANN_HLLC 2
+int mhdgb_set_riemann(mhdgb_solver* h, int solver);
+int mhdgb_get_riemann(const mhdgb_solver* h);   /* the solver in use, or MHDGB_ERR_ARG */
 
 /* GridArray G (mhd.hpp:22-182): cell faces x1a/x2a/x3a, lengths itot/jtot/ktot. */
 int mhdgb_get_grid(const mhdgb_solver* h, double* x1a, double* x2a, double* x3a);
@@ -188,6 +201,36 @@ int mhdgb_diag(mhdgb_solver* h, double out[3]);
  * scalar X = (1+tanh(y/width))/2) written into U; see mhdturbulence_gb300/ic.py. */
 int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, double width, double bx, double amp,
                   double sig, double noise);
+
+/* ---- snapshot output ----
+ * Output(true) of src_cpp_kokkos_host/output.cpp:379-407 for one rank: under root (NULL: "."),
+ * bindata/unf%05d.dat, bindata/grid{1,2,3}D.bin, bindata/field%05d.bin ([10][nz][ny][nx] FP64:
+ * d v1 v2 v3 b1 b2 b3 bp p X1), bindata/field%05d.xmf and, if ascii, ascdata/snap000-%05d.csv
+ * (MPI_IO_Pack/MPI_IO_Write/WriteXDMF/ASC_WRITE, output.cpp:81-386), byte for byte the reference's
+ * files for the same P, time and dt.  time/dt are the values written in the headers
+ * (resolution_mod::time_sim and dt).  The state written is the primitive array the caller
+ * uploaded, if it is still current, else the primitives recovered from U.
+ * mhdgb_output_begin packs the state on the device after every step already enqueued, copies it to
+ * pinned host memory on a second stream and writes the files on a host thread, so steps enqueued
+ * after it overlap the copy and the file writing; mhdgb_output_end waits for that and returns the
+ * writer's status (MHDGB_ERR_IO on a failed write).  A begin while a previous snapshot is still
+ * being written waits for it first.  mhdgb_output = begin + end.  The first call allocates a
+ * device and a pinned host buffer of 80 bytes per cell. */
+int mhdgb_output_begin(mhdgb_solver* h, const char* root, int index, double time, double dt, int ascii);
+int mhdgb_output_end(mhdgb_solver* h);
+int mhdgb_output(mhdgb_solver* h, const char* root, int index, double time, double dt, int ascii);
+
+/* ---- checkpoint / restart ----
+ * No counterpart in the reference, which has none.  save writes the conserved state U (with
+ * ghosts, FieldArray layout), the grid, gam, cfl, the boundary types, the Riemann solver and the
+ * clock (step, time, latest dt and c_h, stop time and step) to one binary file; load restores all of
+ * it into a handle of the same nx, ny, nz and spacing_quirk (any precision).  The next fused step
+ * recovers P from U and
+ * reduces dt and c_h as mhdgb_prepare does, so a run restarted in the same precision continues bit
+ * for bit as if it had not stopped.  Errors: MHDGB_ERR_IO (file), MHDGB_ERR_ARG (not a checkpoint,
+ * or another grid). */
+int mhdgb_checkpoint_save(mhdgb_solver* h, const char* path);
+int mhdgb_checkpoint_load(mhdgb_solver* h, const char* path);
 
 /* ---- ensemble: many independent grids advanced together ----
  * Every member is an ordinary handle (upload/download/init/diag work on it; the ensemble owns it)

@@ -10,6 +10,8 @@
 //                  (mhd.hpp:117-359 of src_cpp_kokkos_host, device variant src_cpp_kokkos_device/mhd.hpp)
 //   boundary_mod:: BoundaryArray, Bs, Br, boundary_xin..boundary_zout, AllocateBoundaryVariables,
 //                  DeallocateBoundaryVariables, SetBoundaryCondition (boundary.hpp:14-145)
+//   Output         the snapshot writer of output.hpp:93 (as mhdgb_ref::Output, and as the global
+//                  Output when MHDGB_REF_OUTPUT is defined, in place of output.cpp)
 // The arrays live on the GPU.  As in the reference's device build, the host mirror of a FieldArray
 // is refreshed with d2h() and sent with h2d() (mhd.hpp:310-315); stages run on the device copies.
 // resolution_mod::dt and hydflux_mod::chg stay the source of truth: ControlTimestep and EvaluateCh
@@ -270,5 +272,26 @@ inline void SetBoundaryCondition(FieldArray<double>&, BoundaryArray<double>&, Bo
   mhdgb_ref::check(mhdgb_set_boundary(mhdgb_ref::handle()), "SetBoundaryCondition");
 }
 }  // namespace boundary_mod
+
+namespace mhdgb_ref {
+// Output(is_forced) of output.cpp:379-407: unless forced, only once time_sim has reached
+// time_out + dtout; writes the current GPU state's snapshot files under the working directory
+// (bindata/, and ascdata/ when config::asciiout), prints the reference's line, advances the index
+// and sets time_out.  The state written is the device P (or U's primitives after steps), so no
+// P.d2h() is needed first.
+inline void Output(bool is_forced) {
+  using namespace resolution_mod;
+  static int index = 0;
+  if (!is_forced && time_sim < time_out + dtout) return;
+  check(mhdgb_output(handle(), ".", index, time_sim, dt, config::asciiout ? 1 : 0), "Output");
+  std::printf("output index=%i, time=%e \n", index, time_sim);
+  index += 1;
+  time_out = time_sim;
+}
+}  // namespace mhdgb_ref
+
+#ifdef MHDGB_REF_OUTPUT
+inline void Output(bool is_forced) { mhdgb_ref::Output(is_forced); }
+#endif
 
 #endif

@@ -14,9 +14,10 @@ _lib = None
 
 MHDGB_FP64, MHDGB_FP64_EXACT, MHDGB_MIXED = 0, 1, 2
 PRECISIONS = {"fp64": MHDGB_FP64, "fp64_exact": MHDGB_FP64_EXACT, "mixed": MHDGB_MIXED}
+RIEMANN = {"hlld": 0, "hlle": 1, "hllc": 2}
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "non-positive rho/p",
           -5: "device wait timed out", -6: "call out of order", -7: "device allocation failed",
-          -8: "grid too large for the fixed scratch"}
+          -8: "grid too large for the fixed scratch", -9: "file output failed"}
 
 # every symbol include/mhdgb.h declares, with (restype, argtypes)
 _dp = C.POINTER(C.c_double)
@@ -44,6 +45,8 @@ SIGNATURES = {
     "mhdgb_extents": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "mhdgb_device_bytes": (C.c_size_t, [_vp]),
     "mhdgb_set_physics": (C.c_int, [_vp, C.c_double, C.c_double, C.POINTER(C.c_int)]),
+    "mhdgb_set_riemann": (C.c_int, [_vp, C.c_int]),
+    "mhdgb_get_riemann": (C.c_int, [_vp]),
     "mhdgb_get_grid": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mhdgb_set_grid": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mhdgb_upload_cons": (C.c_int, [_vp, _dp]),
@@ -57,6 +60,11 @@ SIGNATURES = {
     "mhdgb_download_prim_field": (C.c_int, [_vp, C.c_int, _dp]),
     "mhdgb_control_timestep": (C.c_int, [_vp, _dp]),
     "mhdgb_set_boundary": (C.c_int, [_vp]),
+    "mhdgb_output_begin": (C.c_int, [_vp, C.c_char_p, C.c_int, C.c_double, C.c_double, C.c_int]),
+    "mhdgb_output_end": (C.c_int, [_vp]),
+    "mhdgb_checkpoint_save": (C.c_int, [_vp, C.c_char_p]),
+    "mhdgb_checkpoint_load": (C.c_int, [_vp, C.c_char_p]),
+    "mhdgb_output": (C.c_int, [_vp, C.c_char_p, C.c_int, C.c_double, C.c_double, C.c_int]),
     "mhdgb_fill_ghosts_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), _vp]),
     "mhdgb_evaluate_ch": (C.c_int, [_vp, _dp]),
     "mhdgb_flux": (C.c_int, [_vp, C.c_int]),

@@ -8,6 +8,7 @@ Translation units are compiled in parallel with nvcc:
   csrc/mixed.cu                 FP32-mixed fused steps (fast FP32 div/sqrt), several tile shapes
   csrc/solver.cu                host side of the C ABI (include/mhdgb.h)
   csrc/ghost_noalloc.cu         allocation-free ghost fill on a caller-owned array
+  csrc/output.cpp               writer of the reference's snapshot files (host code)
 and linked into mhdturbulence_gb300/_build/libmhdgb.so (static CUDA runtime).
 """
 from __future__ import annotations
@@ -35,6 +36,7 @@ UNITS = [
     ("mixed.cu", ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("solver.cu", []),
     ("ghost_noalloc.cu", []),
+    ("output.cpp", []),
 ]
 
 

@@ -46,9 +46,11 @@ int variants_fp64(const FusedVariant** out) {
       v_fast64::FusedLauncher<double, 16, 8, 128>::variant(FUSED_FP64),
       v_fast64::FusedLauncher<double, 32, 4, 256>::variant(FUSED_FP64),
       v_fast64::FusedLauncher<double, 16, 8, 256>::variant(FUSED_FP64),
+      // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
+      v_fast64::FusedLauncher<double, 16, 8, 256, 1, true>::variant(FUSED_FP64),
   };
   *out = v;
-  return (int)(sizeof(v) / sizeof(v[0]));
+  return (int)(sizeof(v) / sizeof(v[0])) - 1;  // the last entry is the run-time solver kernel
 }
 
 cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {

@@ -50,7 +50,9 @@ struct FusedSmem {
   static constexpr size_t slx_off = ((size_t)NBUF * PLANE * sizeof(R) + 127) / 128 * 128;
   static constexpr size_t sly_off = slx_off + a16(NSLX * sizeof(R));
   static constexpr size_t slz_off = sly_off + a16(NSLY * sizeof(R));
-  static constexpr size_t fx_off = slz_off + a16(2 * NSLZ * sizeof(R));
+  // three z-slope planes: the current and next plane's, and plane kb-1's at the start of a chunk
+  // (whose column-owned entries then hold the flux through face kb-1/2)
+  static constexpr size_t fx_off = slz_off + a16(3 * NSLZ * sizeof(R));
   static constexpr size_t fy_off = fx_off + a16(NFX * sizeof(R));
   static constexpr size_t fz_off = fy_off + a16(NFY * sizeof(R));
   static constexpr size_t red_off = fz_off + a16(NFZ * sizeof(R));
@@ -243,7 +245,10 @@ __device__ __forceinline__ void update_cell(const DivAcc<float>& acc, const doub
 
 // MINB: CTAs per SM the register allocation must allow (__launch_bounds__); 2 at 256 threads caps
 // a thread at 128 registers, which the FP32 form meets without spills.
-template <class R, int TX, int TY, int NT, int MINB>
+// GEN: false compiles HLLD alone (the tuned tile variants); true reads the Riemann solver from the
+// arguments (one such kernel per form runs HLLE/HLLC), so adding solvers never changes the code,
+// and hence the FMA contraction, of the HLLD kernels.
+template <class R, int TX, int TY, int NT, int MINB, bool GEN>
 __global__ void __launch_bounds__(NT, MINB)
 k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc) {
   using S = FusedSmem<R, TX, TY, NT>;
@@ -308,6 +313,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     const double dt = a.cfl * bitsd(cur_slot.dtmin_bits);
     const double chd = bitsd(cur_slot.chmax_bits);
     const R chg = (R)chd;
+    const int riemann = GEN ? a.riemann : (int)RIEMANN_HLLD;
     const float dtf = (float)dt, chf = (float)chd;
     RedSlot* next = &ctrl->slot[(step + 1) % 3];
     R cmin = R(1e30), cmax = R(0);
@@ -352,30 +358,26 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     __syncthreads();
     if (s_abort) break;
 
+    // z slopes of planes kb-1 (buffer 2) and kb (buffer 0).  The flux through face kb-1/2 is formed
+    // in the first plane's phase B by the same code as every other z face, so a face shared by two
+    // chunks comes out bit for bit the same in both (the result cannot depend on the z-chunking).
     R fz_lo[NCONS];  // flux through face k-1/2 of the owner's column
     int zb = 0;      // slz buffer holding the z slope of the current plane
     if (own) {
       const R *pm2 = plane(kb - 2), *pm1 = plane(kb - 1), *p0 = plane(kb), *pp1 = plane(kb + 1);
-      R pl[NPRIM], pr[NPRIM];
 #pragma unroll
       for (int n = 0; n < NPRIM; n++) {
         const R a2 = PV(pm2, n, oi, oj), a1 = PV(pm1, n, oi, oj), b0 = PV(p0, n, oi, oj), b1 = PV(pp1, n, oi, oj);
-        const R zsm1 = van_leer(b0 - a1, a1 - a2);
-        const R zs0 = van_leer(b1 - b0, b0 - a1);
-        SLZ(0, n, oi, oj) = zs0;
-        pl[n] = left_state(a1, zsm1);
-        pr[n] = right_state(b0, zs0);
+        SLZ(2, n, oi, oj) = van_leer(b0 - a1, a1 - a2);
+        SLZ(0, n, oi, oj) = van_leer(b1 - b0, b0 - a1);
       }
-      face_flux<R, 3>(pl, pr, chg, fz_lo);
     }
-    __syncthreads();  // planes kb-2, kb-1 retired
+    __syncthreads();  // plane kb-2 retired (kb-1 stays until the first plane's faces are formed)
     if (tid == 0) {
       fence_proxy_async();
       if (kb + 2 <= ke + 1) issue(kb + 2);
-      if (kb + 3 <= ke + 1) issue(kb + 3);
     }
     if (kb + 2 <= ke + 1) fills[slot_of(kb + 2)]++;
-    if (kb + 3 <= ke + 1) fills[slot_of(kb + 3)]++;
 
     // work-list sizes (padded to whole warps per sub-list)
     const int nxs = cy * (cx + 2), nys = (cy + 2) * cx, nzs = cy * cx;
@@ -422,8 +424,9 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         }
       }
       __syncthreads();
-      // ---- phase B: face fluxes ----
-      for (int q = tid; q < pxf + pyf + pzf; q += NT) {
+      // ---- phase B: face fluxes (on the first plane also the faces kb-1/2, into slope buffer 2) ----
+      const int nq = pxf + pyf + (k == kb ? 2 * pzf : pzf);
+      for (int q = tid; q < nq; q += NT) {
         R pl[NPRIM], pr[NPRIM], f[NCONS];
         if (q < pxf) {
           if (q < nxf) {
@@ -433,7 +436,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
               pl[n] = left_state(PV(pk, n, i - 1, j), SLX(n, i - 1, j));
               pr[n] = right_state(PV(pk, n, i, j), SLX(n, i, j));
             }
-            face_flux<R, 1>(pl, pr, chg, f);
+            face_flux<R, 1>(pl, pr, chg, f, riemann);
 #pragma unroll
             for (int m = 0; m < NCONS; m++) FXS(m, i, j) = f[m];
           }
@@ -446,28 +449,41 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
               pl[n] = left_state(PV(pk, n, i, j - 1), SLY(n, i, j - 1));
               pr[n] = right_state(PV(pk, n, i, j), SLY(n, i, j));
             }
-            face_flux<R, 2>(pl, pr, chg, f);
+            face_flux<R, 2>(pl, pr, chg, f, riemann);
 #pragma unroll
             for (int m = 0; m < NCONS; m++) FYS(m, i, j) = f[m];
           }
         } else {
-          const int r = q - pxf - pyf;
+          int r = q - pxf - pyf;
+          const bool lower = r >= pzf;  // face kb-1/2 (first plane only)
+          if (lower) r -= pzf;
           if (r < nzf) {
             const int j = r / cx, i = r % cx;
+            const R* pa = lower ? plane(kb - 1) : pk;
+            const R* pb = lower ? pk : pk1;
+            const int sa = lower ? 2 : zb, sb = lower ? zb : (zb ^ 1);
 #pragma unroll
             for (int n = 0; n < NPRIM; n++) {
-              pl[n] = left_state(PV(pk, n, i, j), SLZ(zb, n, i, j));
-              pr[n] = right_state(PV(pk1, n, i, j), SLZ(zb ^ 1, n, i, j));
+              pl[n] = left_state(PV(pa, n, i, j), SLZ(sa, n, i, j));
+              pr[n] = right_state(PV(pb, n, i, j), SLZ(sb, n, i, j));
             }
-            face_flux<R, 3>(pl, pr, chg, f);
+            face_flux<R, 3>(pl, pr, chg, f, riemann);
+            // the lower face overwrites the slopes it alone read (column (i, j) of buffer 2)
 #pragma unroll
-            for (int m = 0; m < NCONS; m++) FZS(m, i, j) = f[m];
+            for (int m = 0; m < NCONS; m++) {
+              if (lower) SLZ(2, m, i, j) = f[m];
+              else FZS(m, i, j) = f[m];
+            }
           }
         }
       }
       __syncthreads();
       // ---- phase C: cell update, recovery, ghost images, candidates ----
       if (own) {
+        if (k == kb) {
+#pragma unroll
+          for (int m = 0; m < NCONS; m++) fz_lo[m] = SLZ(2, m, oi, oj);
+        }
         DivAcc<R> acc;
         const R xi = inv_of<R>(a, 0, ii + NGH);
         const R yi = inv_of<R>(a, 1, (a.quirk ? ii : jj) + NGH);
@@ -492,6 +508,13 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         cmax = smax(cmax, chc);
       }
       __syncthreads();  // plane k and the work buffers retired
+      if (k == kb && kb + 3 <= ke + 1) {  // plane kb-1's slot is free now
+        if (tid == 0) {
+          fence_proxy_async();
+          issue(kb + 3);
+        }
+        fills[slot_of(kb + 3)]++;
+      }
       if (k + 4 <= ke + 1) {
         if (tid == 0) {
           fence_proxy_async();
@@ -559,22 +582,22 @@ __global__ void k_recover(FusedArgs a, int which, RedSlot* slot) {
 }
 
 // Host side of one instantiation of the fused kernel.
-template <class R, int TX, int TY, int NT, int MINB = 1>
+template <class R, int TX, int TY, int NT, int MINB = 1, bool GEN = false>
 struct FusedLauncher {
   using S = FusedSmem<R, TX, TY, NT>;
   static FusedShape shape() { return FusedShape{TX, TY, S::total, NT, (int)sizeof(R), MINB}; }
   static cudaError_t prepare() {
-    return cudaFuncSetAttribute(k_fused_step<R, TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_fused_step<R, TX, TY, NT, MINB, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)S::total);
   }
   static int ctas_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_fused_step<R, TX, TY, NT, MINB>, NT, S::total) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_fused_step<R, TX, TY, NT, MINB, GEN>, NT, S::total) != cudaSuccess)
       return 0;
     return n;
   }
   static cudaError_t launch(const InstanceDesc* desc, LaunchCtrl* lc, int grid, cudaStream_t s) {
-    k_fused_step<R, TX, TY, NT, MINB><<<grid, NT, S::total, s>>>(desc, lc);
+    k_fused_step<R, TX, TY, NT, MINB, GEN><<<grid, NT, S::total, s>>>(desc, lc);
     return cudaGetLastError();
   }
   static FusedVariant variant(FusedKind kind) {

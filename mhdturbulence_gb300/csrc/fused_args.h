@@ -27,6 +27,7 @@ struct FusedArgs {
   double gam, cfl;
   int bc[6];
   int quirk;                           // y/z inverse spacing taken at index i (mhd.cpp:1435-1436)
+  int riemann;                         // RIEMANN_HLLD / _HLLE / _HLLC
   int ntx, nty, nkc, kc;               // tiles in x, y; chunks in z; planes per chunk
   Ctrl* ctrl;
 };

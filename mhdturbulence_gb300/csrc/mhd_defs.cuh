@@ -19,6 +19,10 @@ enum : int { mden = 0, mrv1 = 1, mrv2 = 2, mrv3 = 3, meto = 4, mbm1 = 5, mbm2 = 
 // rotated (normal, tangential-1, tangential-2) aliases of the momentum and field slots
 enum : int { mrvu = 1, mrvv = 2, mrvw = 3, mbmu = 5, mbmv = 6, mbmw = 7 };
 
+// Riemann solvers: HLLD (the C++ path's, mhd.cpp:97-417) and the Fortran variant's alternatives
+// HLLE and HLLC (src_f90_acc_device/mhd.f90:877-1141); values as MHDGB_RIEMANN_* in mhdgb.h.
+enum : int { RIEMANN_HLLD = 0, RIEMANN_HLLE = 1, RIEMANN_HLLC = 2 };
+
 // std::min / std::max of the reference: min(a,b) = (b<a)?b:a, max(a,b) = (a<b)?b:a.
 template <class R> __device__ __forceinline__ R smin(R a, R b) { return (b < a) ? b : a; }
 template <class R> __device__ __forceinline__ R smax(R a, R b) { return (a < b) ? b : a; }

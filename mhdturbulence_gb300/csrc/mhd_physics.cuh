@@ -388,17 +388,105 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   nflux[mbps] = R(0);
 }
 
-// Face flux from the reconstructed left/right primitive states: Prim2Cons of both sides, HLLD,
+// HLLE of the Fortran variant (src_f90_acc_device/mhd.f90:877-907), on the same rotated state/flux
+// vectors as hlld(): one intermediate state between the fastest left- and right-going signals
+// sl = min(0, min(vl,vr) - max(cfl,cfr)), sr = max(0, max(vl,vr) + max(cfl,cfr)).
+template <class R, int DIR>
+__device__ __forceinline__ void hlle(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], R (&nflux)[NCONS]) {
+  const R csl = leftst[mcsp], csr = rigtst[mcsp];
+  const R vl = leftst[mvel], vr = rigtst[mvel];
+  R sl = smin(vl, vr) - smax(csl, csr);
+  sl = smin(R(0), sl);
+  R sr = smax(vl, vr) + smax(csl, csr);
+  sr = smax(R(0), sr);
+  if constexpr (kFast) {
+    const R inv = fdiv(R(1), sr - sl);
+#pragma unroll
+    for (int m = 0; m < NCONS; m++)
+      nflux[m] = (sr * leftst[NCONS + m] - sl * rigtst[NCONS + m] + sl * sr * (rigtst[m] - leftst[m])) * inv;
+  } else {
+#pragma unroll
+    for (int m = 0; m < NCONS; m++)
+      nflux[m] = (sr * leftst[NCONS + m] - sl * rigtst[NCONS + m] + sl * sr * (rigtst[m] - leftst[m])) / (sr - sl);
+  }
+}
+
+// HLLC of the Fortran variant (src_f90_acc_device/mhd.f90:909-1141; Toro, Spruce & Speares): the
+// contact speed sm and total pressure ptst of eqs. 45 and 49, star states with the transverse field
+// scaled by rho*/rho, and the upwind side's flux chosen by the sign of sm.  The Fortran routine
+// reads a passive-scalar star state it never sets; here it is scaled by rho*/rho like the field.
+template <class R, int DIR>
+__device__ __forceinline__ void hllc(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], const R (&Pl)[NPRIM],
+                                     const R (&Pr)[NPRIM], R (&nflux)[NCONS]) {
+  using D = Dir<DIR>;
+  const R rol = leftst[mudn], eel = leftst[muet];
+  const R rxl = leftst[muvu], ryl = leftst[muvv], rzl = leftst[muvw];
+  const R ror = rigtst[mudn], eer = rigtst[muet];
+  const R rxr = rigtst[muvu], ryr = rigtst[muvv], rzr = rigtst[muvw];
+  R vxl, vyl, vzl, vxr, vyr, vzr;
+  if constexpr (kFast) {  // the reconstructed velocities these momenta were formed from
+    vxl = Pl[D::nved]; vyl = Pl[D::nvef]; vzl = Pl[D::nveb];
+    vxr = Pr[D::nved]; vyr = Pr[D::nvef]; vzr = Pr[D::nveb];
+  } else {
+    vxl = leftst[muvu] / leftst[mudn]; vyl = leftst[muvv] / leftst[mudn]; vzl = leftst[muvw] / leftst[mudn];
+    vxr = rigtst[muvu] / rigtst[mudn]; vyr = rigtst[muvv] / rigtst[mudn]; vzr = rigtst[muvw] / rigtst[mudn];
+  }
+  const R scl = leftst[must], scr = rigtst[must];
+  const R byl = leftst[mubv], bzl = leftst[mubw], byr = rigtst[mubv], bzr = rigtst[mubw];
+  const R ptl = leftst[mpre], ptr = rigtst[mpre];
+  const R cfl = leftst[mcsp], cfr = rigtst[mcsp];
+  const R sl = smin(vxl, vxr) - smax(cfl, cfr);
+  const R sr = smax(vxl, vxr) + smax(cfl, cfr);
+  const R sdl = sl - vxl, sdr = sr - vxr;
+  const R rosdl = rol * sdl, rosdr = ror * sdr;
+  const R temp = fdiv(R(1), rosdr - rosdl);
+  const R sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * temp;
+  const R sdml = sl - sm, isdml = fdiv(R(1), sdml);
+  const R sdmr = sr - sm, isdmr = fdiv(R(1), sdmr);
+  const R ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * temp;
+  const R rolst = rol * sdl * isdml;
+  const R rxlst = rolst * sm, rylst = rolst * vyl, rzlst = rolst * vzl;
+  const R bylst = rolst / rol * byl, bzlst = rolst / rol * bzl, sclst = rolst / rol * scl;
+  const R eelst = (sdl * eel - ptl * vxl + ptst * sm) * isdml;
+  const R rorst = rosdr * isdmr;
+  const R rxrst = rorst * sm, ryrst = rorst * vyr, rzrst = rorst * vzr;
+  const R byrst = rorst / ror * byr, bzrst = rorst / ror * bzr, scrst = rorst / ror * scr;
+  const R eerst = (sdr * eer - ptr * vxr + ptst * sm) * isdmr;
+  const R sign1 = copysign(R(1), sm);
+  const R maxs1 = smax(R(0), sign1), mins1 = -smin(R(0), sign1);
+  const R msl = smin(sl, R(0)), msr = smax(sr, R(0));
+  nflux[mden] = (leftst[mfdn] + msl * (rolst - rol)) * maxs1 + (rigtst[mfdn] + msr * (rorst - ror)) * mins1;
+  nflux[meto] = (leftst[mfet] + msl * (eelst - eel)) * maxs1 + (rigtst[mfet] + msr * (eerst - eer)) * mins1;
+  nflux[mrvu] = (leftst[mfvu] + msl * (rxlst - rxl)) * maxs1 + (rigtst[mfvu] + msr * (rxrst - rxr)) * mins1;
+  nflux[mrvv] = (leftst[mfvv] + msl * (rylst - ryl)) * maxs1 + (rigtst[mfvv] + msr * (ryrst - ryr)) * mins1;
+  nflux[mrvw] = (leftst[mfvw] + msl * (rzlst - rzl)) * maxs1 + (rigtst[mfvw] + msr * (rzrst - rzr)) * mins1;
+  nflux[mbmu] = R(0);
+  nflux[mbmv] = (leftst[mfbv] + msl * (bylst - byl)) * maxs1 + (rigtst[mfbv] + msr * (byrst - byr)) * mins1;
+  nflux[mbmw] = (leftst[mfbw] + msl * (bzlst - bzl)) * maxs1 + (rigtst[mfbw] + msr * (bzrst - bzr)) * mins1;
+  nflux[mbps] = R(0);
+  nflux[mst] = (leftst[mfst] + msl * (sclst - scl)) * maxs1 + (rigtst[mfst] + msr * (scrst - scr)) * mins1;
+}
+
+// Face flux from the reconstructed left/right primitive states: Prim2Cons of both sides, the Riemann
+// solver (HLLD as in the C++ path by default; HLLE or HLLC, the Fortran variant's alternatives),
 // then the rotation back to (rho, m1, m2, m3, E, B1, B2, B3, psi, X) order with the GLM pair for
 // the normal field and psi (mhd.cpp:1223-1240 and equivalents).
+// riemann selects the solver (RIEMANN_HLLD / _HLLE / _HLLC); it is the same for a whole launch.
 template <class R, int DIR>
-__device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NPRIM], R chg, R (&F)[NCONS]) {
+__device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NPRIM], R chg, R (&F)[NCONS],
+                                          int riemann = RIEMANN_HLLD) {
   using D = Dir<DIR>;
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
   prim2cons<R, DIR>(Pl, Cl);
   prim2cons<R, DIR>(Pr, Cr);
-  if constexpr (kFast && std::is_same<R, double>::value) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf);
-  else hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
+  if (riemann == RIEMANN_HLLE) {
+    hlle<R, DIR>(Cl, Cr, nf);
+  } else if (riemann == RIEMANN_HLLC) {
+    hllc<R, DIR>(Cl, Cr, Pl, Pr, nf);
+  } else {
+    if constexpr (kFast && std::is_same<R, double>::value) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf);
+    else hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
+  }
   F[mden] = nf[mden];
   F[mrv1] = nf[D::orv1];
   F[mrv2] = nf[D::orv2];

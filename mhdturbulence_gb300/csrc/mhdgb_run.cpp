@@ -3,12 +3,20 @@
 //
 //   mhdgb_run [-n N | -nx X -ny Y -nz Z] [-p fp64|fp64_exact|mixed] [-t TMAX] [-s MAXSTEPS]
 //             [-d DIAG_EVERY] [-o t-prof.csv] [--seed S] [--vshear V] [--bx B] [--amp A] [--noise E]
-//             [--cfl C] [--autotune]
+//             [--cfl C] [--autotune] [--output DIR [--dtout T] [--ascii]]
+//             [--restart FILE] [--checkpoint FILE]
 //
 // Prints the reference's report lines ("sim time [s]:", "time/count/cell :", main.cpp:274-276).
 // With -d > 0 the KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84) is
 // appended to the t-prof.csv file every DIAG_EVERY steps, at the start and at the end; with -d 0
 // (benchmark mode, config::benchmarkmode) only at the start and at the end.
+// With --output the reference's snapshots (Output, output.cpp:379-407) are written under DIR: the
+// forced ones at the start and the end (main.cpp:219, 279) and, with --dtout, one at the first step
+// whose time reaches the previous snapshot's time + T (main.cpp:261).  Snapshots are written
+// asynchronously while the following steps run.
+// --restart starts from a checkpoint (state, grid, physics and clock) instead of the KH set-up;
+// --checkpoint writes one at the end (mhdgb_checkpoint_save / _load).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -59,8 +67,9 @@ int main(int argc, char** argv) {
   long long max_steps = 600000;  // config::stepmax
   int diag_every = 0;
   unsigned long long seed = 1;
-  bool autotune = false;
-  std::string tprof = "t-prof.csv";
+  bool autotune = false, ascii = false;
+  double dtout = 0.0;
+  std::string tprof = "t-prof.csv", outdir, restart, checkpoint;
   for (int a = 1; a < argc; a++) {
     std::string s = argv[a];
     auto next = [&]() -> const char* {
@@ -85,38 +94,73 @@ int main(int argc, char** argv) {
     else if (s == "--noise") noise = std::atof(next());
     else if (s == "--cfl") c.cfl = std::atof(next());
     else if (s == "--autotune") autotune = true;
+    else if (s == "--output") outdir = next();
+    else if (s == "--dtout") dtout = std::atof(next());
+    else if (s == "--ascii") ascii = true;
+    else if (s == "--restart") restart = next();
+    else if (s == "--checkpoint") checkpoint = next();
     else { std::fprintf(stderr, "unknown option %s\n", s.c_str()); return 2; }
   }
   mhdgb_solver* h = nullptr;
   int rc = mhdgb_create(&c, &h);
   if (rc) die(h, rc, "mhdgb_create");
   std::printf("grid size for x y z = %i %i %i\n", c.nx, c.ny, c.nz);
-  if ((rc = mhdgb_init_kh(h, seed, vshear, 0.05, bx, amp, 0.2, noise))) die(h, rc, "mhdgb_init_kh");
+  if (!restart.empty()) {
+    if ((rc = mhdgb_checkpoint_load(h, restart.c_str()))) die(h, rc, "mhdgb_checkpoint_load");
+  } else if ((rc = mhdgb_init_kh(h, seed, vshear, 0.05, bx, amp, 0.2, noise))) {
+    die(h, rc, "mhdgb_init_kh");
+  }
   if (autotune) {
     int best = 0;
     if ((rc = mhdgb_autotune(h, 3, &best))) die(h, rc, "mhdgb_autotune");
   }
+  mhdgb_report r{};
+  if ((rc = mhdgb_sync(h, &r))) die(h, rc, "mhdgb_sync");   // the clock (non-zero after a restart)
+  const long long step0 = r.step;
   TProf prof;
   prof.open(tprof.c_str());
-  prof.write(h, 0.0);
-  if ((rc = mhdgb_set_stop(h, tmax, max_steps))) die(h, rc, "mhdgb_set_stop");
+  prof.write(h, r.time);
+  // Output(forceoutput) at the initial state (resolution_mod::dt is still 0 there on a fresh start).
+  int out_index = 0;
+  double time_out = r.time;
+  const bool output = !outdir.empty();
+  auto snapshot = [&](double t, double dt) {
+    int rc2 = mhdgb_output_begin(h, outdir.c_str(), out_index, t, dt, ascii ? 1 : 0);
+    if (rc2) die(h, rc2, "mhdgb_output_begin");
+    std::printf("output index=%i, time=%e \n", out_index, t);
+    out_index += 1;
+    time_out = t;
+  };
+  if (output) snapshot(r.time, r.dt);
   if ((rc = mhdgb_prepare(h))) die(h, rc, "mhdgb_prepare");
   std::printf("entering main loop\n");
   const auto t0 = std::chrono::high_resolution_clock::now();
-  mhdgb_report r{};
   const int chunk = diag_every > 0 ? diag_every : 256;
   for (;;) {
-    if ((rc = mhdgb_step(h, chunk))) die(h, rc, "mhdgb_step");
-    if ((rc = mhdgb_sync(h, &r))) die(h, rc, "mhdgb_sync");
-    if (diag_every > 0 && !r.done) prof.write(h, r.time);
-    if (r.done) break;
+    // Stop at tmax, or at the first step past the next regular snapshot time.
+    const bool regular = output && dtout > 0.0;
+    const double stop_t = regular ? std::min(tmax, time_out + dtout) : tmax;
+    if ((rc = mhdgb_set_stop(h, stop_t, max_steps))) die(h, rc, "mhdgb_set_stop");
+    for (;;) {
+      if ((rc = mhdgb_step(h, chunk))) die(h, rc, "mhdgb_step");
+      if ((rc = mhdgb_sync(h, &r))) die(h, rc, "mhdgb_sync");
+      if (diag_every > 0 && !r.done) prof.write(h, r.time);
+      if (r.done) break;
+    }
+    if (regular && r.time >= time_out + dtout) snapshot(r.time, r.dt);   // Output(usualoutput)
+    if (r.time > tmax || r.step >= max_steps) break;
   }
   const auto t1 = std::chrono::high_resolution_clock::now();
   const double elapsed = std::chrono::duration<double>(t1 - t0).count();
   std::printf("exiting main loop time=%e, step=%lld\n", r.time, r.step);
   std::printf("sim time [s]: %e\n", elapsed);
-  std::printf("time/count/cell : %e\n", elapsed / ((double)c.nx * c.ny * c.nz) / (double)r.step);
+  std::printf("time/count/cell : %e\n", elapsed / ((double)c.nx * c.ny * c.nz) / (double)(r.step - step0));
   prof.write(h, r.time);
+  if (output) {
+    snapshot(r.time, r.dt);   // Output(forceoutput) at the end
+    if ((rc = mhdgb_output_end(h))) die(h, rc, "mhdgb_output_end");
+  }
+  if (!checkpoint.empty() && (rc = mhdgb_checkpoint_save(h, checkpoint.c_str()))) die(h, rc, "mhdgb_checkpoint_save");
   std::printf("program has been finished\n");
   mhdgb_destroy(h);
   return 0;

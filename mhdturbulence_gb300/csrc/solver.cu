@@ -7,6 +7,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -14,11 +15,13 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
 #include "../../include/mhdgb.h"
 #include "kernels.h"
+#include "output.h"
 
 using namespace mhdgb;
 
@@ -64,6 +67,23 @@ __global__ void k_ctrl_reset(Ctrl* c, int keep_clock) {
   for (int s = 0; s < 3; s++) { c->slot[s].dtmin_bits = DT_RESET; c->slot[s].chmax_bits = CH_RESET; }
   if (!keep_clock) { c->step = 0; c->time = 0.0; c->last_dt = 0.0; c->last_ch = 0.0; }
   c->done = 0;
+  c->status = 0;
+  c->blocks_done = 0;
+  c->work_next = 0;
+}
+
+// Clock of a restart: the step count, time and latest dt/c_h of a checkpoint, with fresh reduction
+// slots (the first step after the restart reduces them again, as prepare does).
+__global__ void k_ctrl_restore(Ctrl* c, unsigned long long step, double time, double last_dt, double last_ch,
+                               double tmax, unsigned long long max_step) {
+  for (int s = 0; s < 3; s++) { c->slot[s].dtmin_bits = DT_RESET; c->slot[s].chmax_bits = CH_RESET; }
+  c->step = step;
+  c->time = time;
+  c->last_dt = last_dt;
+  c->last_ch = last_ch;
+  c->tmax = tmax;
+  c->max_step = max_step;
+  c->done = (time > tmax || step >= max_step) ? 1u : 0u;
   c->status = 0;
   c->blocks_done = 0;
   c->work_next = 0;
@@ -141,8 +161,9 @@ struct mhdgb_solver {
   // host state
   std::vector<double> x1a, x2a, x3a;
   CUtensorMap tmap[2];
-  const FusedVariant* vars = nullptr;  // compiled tile shapes of this precision
-  int nvars = 0, vidx = 0;             // and the one in use
+  const FusedVariant* vars = nullptr;  // compiled HLLD tile shapes of this precision; vars[nvars] is
+  int nvars = 0, vidx = 0;             // the run-time solver kernel; vidx: the kernel in use
+  int hlld_vidx = 0;                   // the HLLD variant to return to from HLLE/HLLC
   int grid = 0, ntx = 0, nty = 0, nkc = 0, kc = 0;
   long long cur_step = 0;    // device step count as of the last sync (selects the current P)
   bool have_state = false;   // U uploaded
@@ -155,7 +176,17 @@ struct mhdgb_solver {
   LaunchCtrl* d_lc = nullptr;
   double* stage = nullptr;         // dense host-layout staging buffer (allocated on first transfer)
   bool own_stream = true;          // false for the members of an ensemble (they share its stream)
+  int riemann = 0;                 // MHDGB_RIEMANN_*
+  unsigned desc_version = 0;       // bumped whenever the kernel arguments change (ensembles re-read)
   std::string err;
+  // snapshot output (allocated on first use): device pack -> copy stream -> pinned host -> writer
+  double* d_snap = nullptr;
+  double* h_snap = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_packed = nullptr, ev_copied = nullptr;
+  std::thread writer;
+  int writer_rc = MHDGB_OK;
+  std::string writer_err;
 };
 
 namespace {
@@ -388,6 +419,7 @@ FusedArgs fused_args(mhdgb_solver* h) {
   a.cfl = h->cfg.cfl;
   for (int q = 0; q < 6; q++) a.bc[q] = h->cfg.bc[q];
   a.quirk = h->cfg.spacing_quirk;
+  a.riemann = h->riemann;
   a.ntx = h->ntx; a.nty = h->nty; a.nkc = h->nkc; a.kc = h->kc;
   a.ctrl = h->ctrl;
   return a;
@@ -406,6 +438,7 @@ InstanceDesc host_desc(mhdgb_solver* h, int item_begin) {
 
 // The handle as a one-instance launch: descriptor and launch control in device memory.
 int upload_desc(mhdgb_solver* h) {
+  h->desc_version++;
   const InstanceDesc d = host_desc(h, 0);
   const LaunchCtrl lc{0u, 0u, 1u, (unsigned)d.nitems};
   CK(h, cudaMemcpyAsync(h->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, h->stream));
@@ -423,12 +456,13 @@ int launch_one(mhdgb_solver* h) {
 // kc_fixed > 0 sets the planes per work item directly (ensembles keep items of similar size);
 // otherwise the z chunks give about items_per_cta work items per CTA.
 int use_variant(mhdgb_solver* h, int idx, int items_per_cta, int kc_fixed = 0) {
-  if (idx < 0 || idx >= h->nvars) return fail(h, MHDGB_ERR_ARG, "no such variant");
+  if (idx < 0 || idx > h->nvars) return fail(h, MHDGB_ERR_ARG, "no such variant");
   const FusedVariant& v = h->vars[idx];
   CK(h, v.prepare());
   const int cps = v.ctas_per_sm();
   if (cps < 1) return fail(h, MHDGB_ERR_CUDA, "fused kernel variant does not fit on an SM");
   h->vidx = idx;
+  if (idx < h->nvars) h->hlld_vidx = idx;
   h->shape = v.shape;
   h->grid = h->nsm * cps;
   const Layout& L = h->L;
@@ -531,6 +565,7 @@ const char* mhdgb_status_string(int s) {
     case MHDGB_ERR_STATE: return "call out of order";
     case MHDGB_ERR_NOMEM: return "device allocation failed";
     case MHDGB_ERR_SCRATCH: return "grid too large for the fixed scratch of mhdgb_fill_ghosts_noalloc";
+    case MHDGB_ERR_IO: return "file output failed";
     default: return "unknown status";
   }
 }
@@ -614,14 +649,21 @@ int mhdgb_create(const mhdgb_config* cfg, mhdgb_solver** out) { return create_im
 
 int mhdgb_destroy(mhdgb_solver* h) {
   if (!h) return MHDGB_OK;
+  if (h->writer.joinable()) h->writer.join();
   cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   destroy_graph(h);
   void* ptrs[] = {h->U, h->P64[0], h->P64[1], h->P32[0], h->P32[1], h->F[0], h->F[1], h->F[2], h->pack,
                   h->xinv, h->yinv, h->zinv, h->dxs, h->dys, h->dzs, h->xinvf, h->yinvf, h->zinvf,
-                  h->dxsf, h->dysf, h->dzsf, h->scal, h->sslot, h->ctrl, h->d_desc, h->d_lc, h->stage};
+                  h->dxsf, h->dysf, h->dzsf, h->scal, h->sslot, h->ctrl, h->d_desc, h->d_lc, h->stage,
+                  h->d_snap};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (h->h_snap) cudaFreeHost(h->h_snap);
+  if (h->ev_packed) cudaEventDestroy(h->ev_packed);
+  if (h->ev_copied) cudaEventDestroy(h->ev_copied);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return MHDGB_OK;
@@ -663,6 +705,21 @@ int mhdgb_set_physics(mhdgb_solver* h, double gam, double cfl, const int* bc) {
   destroy_graph(h);
   return upload_desc(h);
 }
+
+int mhdgb_set_riemann(mhdgb_solver* h, int solver) {
+  if (!h || solver < MHDGB_RIEMANN_HLLD || solver > MHDGB_RIEMANN_HLLC) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = settle(h))) return rc;
+  if (h->riemann == solver) return MHDGB_OK;
+  h->riemann = solver;
+  // HLLD runs on the tuned HLLD variants, HLLE/HLLC on the run-time solver kernel
+  const int want = solver == MHDGB_RIEMANN_HLLD ? h->hlld_vidx : h->nvars;
+  if (want != h->vidx) return use_variant(h, want, 4);
+  destroy_graph(h);
+  return upload_desc(h);
+}
+
+int mhdgb_get_riemann(const mhdgb_solver* h) { return h ? h->riemann : MHDGB_ERR_ARG; }
 
 int mhdgb_set_grid(mhdgb_solver* h, const double* x1a, const double* x2a, const double* x3a) {
   if (!h || !x1a || !x2a || !x3a) return MHDGB_ERR_ARG;
@@ -810,7 +867,7 @@ int mhdgb_flux(mhdgb_solver* h, int dir) {
   if (!h || dir < 1 || dir > 3) return MHDGB_ERR_ARG;
   int rc = set_device(h);
   if (rc || (rc = ensure_p64(h))) return rc;
-  CK(h, launch_flux(dir, h->P64[cur_index(h)], h->F[dir - 1], h->L, h->scal + 1, h->stream));
+  CK(h, launch_flux(dir, h->P64[cur_index(h)], h->F[dir - 1], h->L, h->scal + 1, h->riemann, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   return MHDGB_OK;
 }
@@ -1065,9 +1122,13 @@ int mhdgb_variant_info(const mhdgb_solver* h, int idx, int* tx, int* ty, int* th
 }
 
 int mhdgb_select_variant(mhdgb_solver* h, int idx) {
-  if (!h) return MHDGB_ERR_ARG;
+  if (!h || idx < 0 || idx >= h->nvars) return MHDGB_ERR_ARG;
   int rc = set_device(h);
   if (rc || (rc = mhdgb_sync(h, nullptr)) == MHDGB_ERR_CUDA) return rc;
+  if (h->riemann != MHDGB_RIEMANN_HLLD) {  // HLLE/HLLC keep their kernel; the choice applies to HLLD
+    h->hlld_vidx = idx;
+    return MHDGB_OK;
+  }
   const bool was_prepared = h->prepared;
   if ((rc = use_variant(h, idx, 4))) return rc;
   h->prepared = was_prepared;  // the P buffers and reduction slots do not depend on the tile shape
@@ -1079,6 +1140,10 @@ int mhdgb_autotune(mhdgb_solver* h, int steps, int* best) {
   int rc = set_device(h);
   if (rc) return rc;
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "autotune needs an uploaded state");
+  if (h->riemann != MHDGB_RIEMANN_HLLD) {  // one kernel runs HLLE/HLLC: nothing to choose
+    if (best) *best = h->hlld_vidx;
+    return MHDGB_OK;
+  }
   Ctrl saved;
   if ((rc = read_ctrl(h, &saved))) return rc;
   const Layout& L = h->L;
@@ -1182,12 +1247,15 @@ struct mhdgb_ensemble {
   int nsm = 0;
   std::vector<mhdgb_solver*> m;
   const FusedVariant* vars = nullptr;
-  int nvars = 0, vidx = 0, grid = 0;
+  int nvars = 0, vidx = 0, grid = 0;   // vidx: the HLLD tile variant selected
+  int active = 0;                      // the kernel launched: vidx, or nvars (run-time solver) when
+                                       // a member uses HLLE/HLLC
   int kc = 8;                       // planes per work item: similar-sized items across grids
   InstanceDesc* d_desc = nullptr;
   LaunchCtrl* d_lc = nullptr;
   int total_items = 0;
   cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned> desc_seen;  // members' desc_version as last copied into d_desc
   std::string err;
 };
 
@@ -1211,19 +1279,29 @@ int ens_member_rc(mhdgb_ensemble* e, int i, int rc) {
 }
 
 // Use tile shape idx for every member and rebuild the launch's instance table.
+bool ens_any_general_solver(const mhdgb_ensemble* e) {
+  for (const auto* h : e->m)
+    if (h->riemann != MHDGB_RIEMANN_HLLD) return true;
+  return false;
+}
+
 int ens_use_variant(mhdgb_ensemble* e, int idx) {
   if (idx < 0 || idx >= e->nvars) return efail(e, MHDGB_ERR_ARG, "no such variant");
+  const int eff = ens_any_general_solver(e) ? e->nvars : idx;
   std::vector<InstanceDesc> d(e->m.size());
   int begin = 0;
   for (size_t i = 0; i < e->m.size(); i++) {
     const bool was = e->m[i]->prepared;
-    int rc = use_variant(e->m[i], idx, 4, e->kc);
+    int rc = use_variant(e->m[i], eff, 4, e->kc);
     if (rc) return ens_member_rc(e, (int)i, rc);
     e->m[i]->prepared = was;
     d[i] = host_desc(e->m[i], begin);
     begin += d[i].nitems;
   }
+  e->desc_seen.resize(e->m.size());
+  for (size_t i = 0; i < e->m.size(); i++) e->desc_seen[i] = e->m[i]->desc_version;
   e->vidx = idx;
+  e->active = eff;
   e->total_items = begin;
   e->grid = e->m[0]->grid;
   const LaunchCtrl lc{0u, 0u, (unsigned)e->m.size(), (unsigned)begin};
@@ -1236,11 +1314,19 @@ int ens_use_variant(mhdgb_ensemble* e, int idx) {
 }
 
 int ens_launch(mhdgb_ensemble* e) {
-  ECK(e, e->vars[e->vidx].launch(e->d_desc, e->d_lc, e->grid, e->stream));
+  ECK(e, e->vars[e->active].launch(e->d_desc, e->d_lc, e->grid, e->stream));
   return MHDGB_OK;
 }
 
 int ens_prepare_all(mhdgb_ensemble* e, bool force) {
+  // a member whose arguments changed (mhdgb_set_physics, mhdgb_set_riemann) since the ensemble's
+  // descriptors were built: rebuild them all
+  for (size_t i = 0; i < e->m.size(); i++)
+    if (i >= e->desc_seen.size() || e->desc_seen[i] != e->m[i]->desc_version) {
+      int rc = ens_use_variant(e, e->vidx);
+      if (rc) return rc;
+      break;
+    }
   for (size_t i = 0; i < e->m.size(); i++) {
     if (!force && e->m[i]->prepared) continue;
     int rc = mhdgb_prepare(e->m[i]);
@@ -1400,6 +1486,10 @@ int mhdgb_ensemble_time_steps(mhdgb_ensemble* e, int nsteps, double* ms) {
 int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best) {
   if (!e || steps < 1) return MHDGB_ERR_ARG;
   if (cudaSetDevice(e->device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  if (ens_any_general_solver(e)) {  // HLLE/HLLC members: the one run-time solver kernel runs all
+    if (best) *best = e->vidx;
+    return MHDGB_OK;
+  }
   // keep every member's U and control block, time each tile shape, restore
   std::vector<Ctrl> saved(e->m.size());
   for (size_t i = 0; i < e->m.size(); i++) {
@@ -1437,6 +1527,196 @@ int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best) {
   }
   if ((rc = ens_use_variant(e, bidx)) || (rc = restore())) return rc;
   if (best) *best = bidx;
+  return MHDGB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Snapshot output (Output, src_cpp_kokkos_host/output.cpp:379-407)
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+int join_writer(mhdgb_solver* h) {
+  if (!h->writer.joinable()) return MHDGB_OK;
+  h->writer.join();
+  if (h->writer_rc) return fail(h, h->writer_rc, h->writer_err);
+  return MHDGB_OK;
+}
+
+int ensure_snapshot_bufs(mhdgb_solver* h) {
+  const size_t n = (size_t)NSNAP * h->L.nx * h->L.ny * h->L.nz;
+  if (!h->d_snap && dalloc(h, &h->d_snap, n) != cudaSuccess) return fail(h, MHDGB_ERR_NOMEM, "snapshot buffer");
+  if (!h->h_snap && cudaMallocHost((void**)&h->h_snap, n * sizeof(double)) != cudaSuccess) {
+    h->h_snap = nullptr;
+    return fail(h, MHDGB_ERR_NOMEM, "pinned snapshot buffer");
+  }
+  if (!h->copy_stream) CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  if (!h->ev_packed) CK(h, cudaEventCreateWithFlags(&h->ev_packed, cudaEventDisableTiming));
+  if (!h->ev_copied) CK(h, cudaEventCreateWithFlags(&h->ev_copied, cudaEventDisableTiming));
+  return MHDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhdgb_output_begin(mhdgb_solver* h, const char* root, int index, double time, double dt, int ascii) {
+  if (!h || index < 0 || index > 99999) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = join_writer(h))) return rc;
+  if (!h->have_state && !h->p_user) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
+  if ((rc = ensure_snapshot_bufs(h))) return rc;
+  // A primitive array the caller uploaded is written as it is (the reference writes its P, which
+  // for the initial state is GenerateProblem's); otherwise the primitives are recovered from U in
+  // stream order, after every step already enqueued.
+  const double* P = h->p_user ? h->P64[cur_index(h)] : nullptr;
+  CK(h, launch_snapshot(h->U, P, h->L, h->cfg.gam, h->d_snap, h->stream));
+  CK(h, cudaEventRecord(h->ev_packed, h->stream));
+  CK(h, cudaStreamWaitEvent(h->copy_stream, h->ev_packed, 0));
+  const size_t bytes = (size_t)NSNAP * h->L.nx * h->L.ny * h->L.nz * sizeof(double);
+  CK(h, cudaMemcpyAsync(h->h_snap, h->d_snap, bytes, cudaMemcpyDeviceToHost, h->copy_stream));
+  CK(h, cudaEventRecord(h->ev_copied, h->copy_stream));
+  SnapshotMeta m;
+  m.root = root ? root : ".";
+  m.index = index;
+  m.time = time;
+  m.dt = dt;
+  m.ascii = ascii != 0;
+  m.nx = h->L.nx; m.ny = h->L.ny; m.nz = h->L.nz;
+  m.x1a = h->x1a; m.x2a = h->x2a; m.x3a = h->x3a;
+  h->writer_rc = MHDGB_OK;
+  h->writer_err.clear();
+  h->writer = std::thread([h, m = std::move(m)]() {
+    cudaSetDevice(h->cfg.device);
+    const cudaError_t e = cudaEventSynchronize(h->ev_copied);
+    if (e != cudaSuccess) {
+      h->writer_rc = MHDGB_ERR_CUDA;
+      h->writer_err = std::string("snapshot copy: ") + cudaGetErrorString(e);
+      return;
+    }
+    std::string err;
+    if (write_snapshot_files(m, h->h_snap, &err)) {
+      h->writer_rc = MHDGB_ERR_IO;
+      h->writer_err = err;
+    }
+  });
+  return MHDGB_OK;
+}
+
+int mhdgb_output_end(mhdgb_solver* h) {
+  if (!h) return MHDGB_ERR_ARG;
+  return join_writer(h);
+}
+
+int mhdgb_output(mhdgb_solver* h, const char* root, int index, double time, double dt, int ascii) {
+  const int rc = mhdgb_output_begin(h, root, index, time, dt, ascii);
+  return rc ? rc : mhdgb_output_end(h);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Checkpoint / restart (the reference has none).  File layout, little endian:
+//   char[8] "MHDGBCK1" | int32 version, nx, ny, nz, precision, spacing_quirk, bc[6], riemann |
+//   float64 x1min, x1max, x2min, x2max, x3min, x3max, gam, cfl |
+//   int64 step | uint64 max_step | float64 time, last_dt, last_ch, tmax |
+//   float64 x1a[itot], x2a[jtot], x3a[ktot] | float64 U[ktot][jtot][10][itot] (FieldArray layout)
+// ---------------------------------------------------------------------------------------------
+namespace {
+constexpr char kCkMagic[8] = {'M', 'H', 'D', 'G', 'B', 'C', 'K', '1'};
+constexpr int kCkVersion = 2;
+
+struct CkHead {
+  int32_t ints[13];   // version, nx, ny, nz, precision, spacing_quirk, bc[6], riemann
+  double reals[8];    // domain, gam, cfl
+  int64_t step;
+  uint64_t max_step;
+  double clock[4];    // time, last_dt, last_ch, tmax
+};
+
+bool wr(FILE* f, const void* p, size_t n) { return std::fwrite(p, 1, n, f) == n; }
+bool rd(FILE* f, void* p, size_t n) { return std::fread(p, 1, n, f) == n; }
+}  // namespace
+
+extern "C" {
+
+int mhdgb_checkpoint_save(mhdgb_solver* h, const char* path) {
+  if (!h || !path) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = settle(h))) return rc;
+  if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state to checkpoint");
+  Ctrl c;
+  if ((rc = read_ctrl(h, &c))) return rc;
+  const Layout& L = h->L;
+  std::vector<double> U((size_t)NCONS * L.itot * L.jtot * L.ktot);
+  if ((rc = download_u(h, U.data()))) return rc;
+  CK(h, cudaStreamSynchronize(h->stream));
+  CkHead hd{};
+  const mhdgb_config& g = h->cfg;
+  const int32_t ints[13] = {kCkVersion, g.nx, g.ny, g.nz, g.precision, g.spacing_quirk,
+                            g.bc[0], g.bc[1], g.bc[2], g.bc[3], g.bc[4], g.bc[5], h->riemann};
+  std::copy(ints, ints + 13, hd.ints);
+  const double reals[8] = {g.x1min, g.x1max, g.x2min, g.x2max, g.x3min, g.x3max, g.gam, g.cfl};
+  std::copy(reals, reals + 8, hd.reals);
+  hd.step = (int64_t)c.step;
+  hd.max_step = c.max_step;
+  hd.clock[0] = c.time; hd.clock[1] = c.last_dt; hd.clock[2] = c.last_ch; hd.clock[3] = c.tmax;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(h, MHDGB_ERR_IO, std::string("cannot create ") + path);
+  bool ok = wr(f, kCkMagic, 8) && wr(f, hd.ints, sizeof(hd.ints)) && wr(f, hd.reals, sizeof(hd.reals)) &&
+            wr(f, &hd.step, 8) && wr(f, &hd.max_step, 8) && wr(f, hd.clock, sizeof(hd.clock)) &&
+            wr(f, h->x1a.data(), 8 * h->x1a.size()) && wr(f, h->x2a.data(), 8 * h->x2a.size()) &&
+            wr(f, h->x3a.data(), 8 * h->x3a.size()) && wr(f, U.data(), 8 * U.size());
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return fail(h, MHDGB_ERR_IO, std::string("cannot write ") + path);
+  return MHDGB_OK;
+}
+
+int mhdgb_checkpoint_load(mhdgb_solver* h, const char* path) {
+  if (!h || !path) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc || (rc = settle(h))) return rc;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(h, MHDGB_ERR_IO, std::string("cannot open ") + path);
+  char magic[8];
+  CkHead hd{};
+  bool ok = rd(f, magic, 8) && std::equal(magic, magic + 8, kCkMagic) && rd(f, hd.ints, sizeof(hd.ints)) &&
+            rd(f, hd.reals, sizeof(hd.reals)) && rd(f, &hd.step, 8) && rd(f, &hd.max_step, 8) &&
+            rd(f, hd.clock, sizeof(hd.clock)) && hd.ints[0] == kCkVersion;
+  if (!ok) {
+    std::fclose(f);
+    return fail(h, MHDGB_ERR_ARG, std::string(path) + " is not a checkpoint of this library");
+  }
+  const mhdgb_config& g = h->cfg;
+  if (hd.ints[1] != g.nx || hd.ints[2] != g.ny || hd.ints[3] != g.nz || hd.ints[5] != g.spacing_quirk) {
+    std::fclose(f);
+    return fail(h, MHDGB_ERR_ARG, "checkpoint grid " + std::to_string(hd.ints[1]) + "x" + std::to_string(hd.ints[2]) +
+                                      "x" + std::to_string(hd.ints[3]) + " (or its spacing_quirk) differs from the handle's");
+  }
+  const Layout& L = h->L;
+  std::vector<double> x1a(L.itot), x2a(L.jtot), x3a(L.ktot), U((size_t)NCONS * L.itot * L.jtot * L.ktot);
+  ok = rd(f, x1a.data(), 8 * x1a.size()) && rd(f, x2a.data(), 8 * x2a.size()) && rd(f, x3a.data(), 8 * x3a.size()) &&
+       rd(f, U.data(), 8 * U.size());
+  std::fclose(f);
+  if (!ok) return fail(h, MHDGB_ERR_IO, std::string(path) + " is truncated");
+  const int bc[6] = {hd.ints[6], hd.ints[7], hd.ints[8], hd.ints[9], hd.ints[10], hd.ints[11]};
+  if ((rc = mhdgb_set_physics(h, hd.reals[6], hd.reals[7], bc))) return rc;
+  if ((rc = mhdgb_set_riemann(h, hd.ints[12]))) return rc;
+  h->cfg.x1min = hd.reals[0]; h->cfg.x1max = hd.reals[1];
+  h->cfg.x2min = hd.reals[2]; h->cfg.x2max = hd.reals[3];
+  h->cfg.x3min = hd.reals[4]; h->cfg.x3max = hd.reals[5];
+  if ((rc = mhdgb_set_grid(h, x1a.data(), x2a.data(), x3a.data()))) return rc;
+  if ((rc = upload_u(h, U.data()))) return rc;
+  k_ctrl_restore<<<1, 1, 0, h->stream>>>(h->ctrl, (unsigned long long)hd.step, hd.clock[0], hd.clock[1], hd.clock[2],
+                                          hd.clock[3], hd.max_step);
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->cur_step = (long long)hd.step;
+  h->have_state = true;
+  h->prepared = false;
+  h->p64_valid = false;
+  h->p_user = false;
   return MHDGB_OK;
 }
 

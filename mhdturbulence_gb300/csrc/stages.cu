@@ -20,7 +20,7 @@ namespace v_exact {
 // k in [ks, ke+dk] (mhd.cpp:1205, 1288, 1371); the flux is stored at the face's upper cell index.
 template <int DIR>
 __global__ void k_flux(const double* __restrict__ P, double* __restrict__ F, Layout L,
-                       const double* __restrict__ chg_ptr) {
+                       const double* __restrict__ chg_ptr, int riemann) {
   constexpr int di = DIR == 1, dj = DIR == 2, dk = DIR == 3;
   const int nfx = L.nx + di, nfy = L.ny + dj, nfz = L.nz + dk;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -44,7 +44,7 @@ __global__ void k_flux(const double* __restrict__ P, double* __restrict__ F, Lay
     Pr[n] = right_state(R1[n], van_leer(R2[n] - R1[n], R1[n] - L2[n]));
   }
   double f[NCONS];
-  face_flux<double, DIR>(Pl, Pr, chg, f);
+  face_flux<double, DIR>(Pl, Pr, chg, f, riemann);
 #pragma unroll
   for (int m = 0; m < NCONS; m++) F[L.at(NCONS, m, k, j, i)] = f[m];
 }
@@ -104,7 +104,34 @@ __global__ void k_update_prim(const double* __restrict__ U, double* __restrict__
   for (int n = 0; n < NPRIM; n++) P[L.at(NPRIM, n, k, j, i)] = p[n];
 }
 
-// Interior min of the CFL time and max of the signal speed (mhd.cpp:1539-1554, 1586-1604) into
+// Snapshot of the interior primitives in the order of the reference's output (MPI_IO_Pack,
+// output.cpp:247-260): out[v][k][j][i] (dense nz*ny*nx per variable) for v = d, v1, v2, v3, b1, b2,
+// b3, bp, p, X1.  Copies P when given, else recovers the primitives from U with UpdatePrimitvP's
+// arithmetic (the values P holds after a step).  One thread per interior cell, i fastest.
+__global__ void k_snapshot(const double* __restrict__ U, const double* __restrict__ P, Layout L, double gam,
+                           double* __restrict__ out) {
+  const long long ncell = (long long)L.nx * L.ny * L.nz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncell) return;
+  const int i = NGH + (int)(t % L.nx);
+  const int j = NGH + (int)((t / L.nx) % L.ny);
+  const int k = NGH + (int)(t / ((long long)L.nx * L.ny));
+  double p[NPRIM];
+  if (P) {
+#pragma unroll
+    for (int n = 0; n < NPRIM; n++) p[n] = P[L.at(NPRIM, n, k, j, i)];
+  } else {
+    double u[NCONS];
+#pragma unroll
+    for (int m = 0; m < NCONS; m++) u[m] = U[L.at(NCONS, m, k, j, i)];
+    cons2prim<double>(u, gam, p);
+  }
+  const int order[NSNAP] = {nden, nve1, nve2, nve3, nbm1, nbm2, nbm3, nbps, npre, nst};
+#pragma unroll
+  for (int v = 0; v < NSNAP; v++) out[v * ncell + t] = p[order[v]];
+}
+
+
 // a reduction slot; cells with a non-finite value, rho <= 0 or p <= 0 raise status bits.
 __global__ void k_reduce_dt_ch(const double* __restrict__ P, Layout L, const double* __restrict__ dxs,
                                const double* __restrict__ dys, const double* __restrict__ dzs,
@@ -240,11 +267,12 @@ using namespace v_exact;
 
 static inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-cudaError_t launch_flux(int dir, const double* P, double* F, const Layout& L, const double* chg, cudaStream_t s) {
+cudaError_t launch_flux(int dir, const double* P, double* F, const Layout& L, const double* chg, int riemann,
+                        cudaStream_t s) {
   const int bs = 128;
-  if (dir == 1) k_flux<1><<<nblk((long long)(L.nx + 1) * L.ny * L.nz, bs), bs, 0, s>>>(P, F, L, chg);
-  else if (dir == 2) k_flux<2><<<nblk((long long)L.nx * (L.ny + 1) * L.nz, bs), bs, 0, s>>>(P, F, L, chg);
-  else k_flux<3><<<nblk((long long)L.nx * L.ny * (L.nz + 1), bs), bs, 0, s>>>(P, F, L, chg);
+  if (dir == 1) k_flux<1><<<nblk((long long)(L.nx + 1) * L.ny * L.nz, bs), bs, 0, s>>>(P, F, L, chg, riemann);
+  else if (dir == 2) k_flux<2><<<nblk((long long)L.nx * (L.ny + 1) * L.nz, bs), bs, 0, s>>>(P, F, L, chg, riemann);
+  else k_flux<3><<<nblk((long long)L.nx * L.ny * (L.nz + 1), bs), bs, 0, s>>>(P, F, L, chg, riemann);
   return cudaGetLastError();
 }
 
@@ -290,6 +318,13 @@ cudaError_t launch_reset_slot(RedSlot* slot, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_snapshot(const double* U, const double* P, const Layout& L, double gam, double* out,
+                            cudaStream_t s) {
+  const int bs = 256;
+  k_snapshot<<<nblk((long long)L.nx * L.ny * L.nz, bs), bs, 0, s>>>(U, P, L, gam, out);
+  return cudaGetLastError();
+}
+
 size_t pack_buffer_doubles(const Layout& L) {
   return 2 * ((size_t)NPRIM * L.ktot * L.jtot * NGH + (size_t)NPRIM * L.ktot * NGH * L.itot +
               (size_t)NPRIM * NGH * L.jtot * L.itot);
@@ -314,9 +349,11 @@ namespace detail {
 int variants_exact(const FusedVariant** out) {
   static const FusedVariant v[] = {
       v_exact::FusedLauncher<double, 32, 4, 128>::variant(FUSED_FP64_EXACT),
+      // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
+      v_exact::FusedLauncher<double, 32, 4, 128, 1, true>::variant(FUSED_FP64_EXACT),
   };
   *out = v;
-  return (int)(sizeof(v) / sizeof(v[0]));
+  return (int)(sizeof(v) / sizeof(v[0])) - 1;  // the last entry is the run-time solver kernel
 }
 cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
   return v_exact::recover_launch<double>(a, which, slot, nsm, s);

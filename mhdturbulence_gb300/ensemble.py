@@ -52,6 +52,8 @@ class Ensemble:
             self.members.append(Solver(sp["nx"], sp["ny"], sp["nz"], precision=precision, device=device,
                                        gam=gam, cfl=cfl, domain=sp.get("domain", ic.KH_DOMAIN),
                                        bc=sp.get("bc", ic.KH_BC), _borrow=h))
+            if sp.get("riemann", "hlld") != "hlld":
+                self.members[-1].set_riemann(sp["riemann"])
 
     def _ck(self, rc, what):
         if rc != 0:

@@ -7,11 +7,12 @@ reference FieldArray layout, shape (ktot, jtot, nv, itot) (see ic.py).  Errors r
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
 from . import ic
-from ._lib import PRECISIONS, Config, MhdgbError, Report, lib
+from ._lib import PRECISIONS, RIEMANN, Config, MhdgbError, Report, lib
 
 
 def make_config(nx, ny, nz, domain=ic.KH_DOMAIN, bc=ic.KH_BC, gam=5.0 / 3.0, cfl=0.05, precision="fp64",
@@ -40,10 +41,11 @@ class Solver:
     precision: "fp64" (FMA-contracted FP64), "fp64_exact" (separately rounded, the reference's
     arithmetic bit for bit) or "mixed" (FP32 reconstruction/Riemann solve, FP64 state, update,
     pressure recovery and reductions).  spacing_quirk reproduces mhd.cpp:1435-1436 (y/z spacing
-    taken at index i in UpdateConservU)."""
+    taken at index i in UpdateConservU).  riemann: "hlld" (the C++ path's), "hlle" or "hllc" (the
+    Fortran variant's alternatives)."""
 
     def __init__(self, nx, ny, nz, domain=ic.KH_DOMAIN, bc=ic.KH_BC, gam=5.0 / 3.0, cfl=0.05,
-                 precision="fp64", spacing_quirk=False, device=0, _borrow=None):
+                 precision="fp64", spacing_quirk=False, device=0, riemann="hlld", _borrow=None):
         self._L = lib()
         self._owned = _borrow is None
         cfg = make_config(nx, ny, nz, domain, bc, gam, cfl, precision, spacing_quirk, device)
@@ -57,6 +59,16 @@ class Solver:
             raise MhdgbError(rc, "mhdgb_create failed")
         self._h = h
         self._setup(nx, ny, nz, precision, cfg)
+        if riemann != "hlld":
+            self.set_riemann(riemann)
+
+    def set_riemann(self, name):
+        self._ck(self._L.mhdgb_set_riemann(self._h, RIEMANN[name]), "set_riemann")
+
+    @property
+    def riemann(self) -> str:
+        code = self._L.mhdgb_get_riemann(self._h)
+        return {v: k for k, v in RIEMANN.items()}[code]
 
     def _setup(self, nx, ny, nz, precision, cfg):
         h = self._h
@@ -231,6 +243,26 @@ class Solver:
         out = np.zeros(3)
         self._ck(self._L.mhdgb_diag(self._h, _dptr(out)), "diag")
         return out
+
+    # -- snapshot output (Output, output.cpp:379-407) --
+    def output_begin(self, root, index, time, dt, ascii=False):
+        """Start writing snapshot `index` of the current state under root (bindata/, ascdata/);
+        steps issued afterwards overlap the copy and the file writing."""
+        self._ck(self._L.mhdgb_output_begin(self._h, os.fsencode(root), index, time, dt, 1 if ascii else 0),
+                 "output_begin")
+
+    def output_end(self):
+        self._ck(self._L.mhdgb_output_end(self._h), "output_end")
+
+    # -- checkpoint / restart --
+    def checkpoint_save(self, path):
+        self._ck(self._L.mhdgb_checkpoint_save(self._h, os.fsencode(path)), "checkpoint_save")
+
+    def checkpoint_load(self, path):
+        self._ck(self._L.mhdgb_checkpoint_load(self._h, os.fsencode(path)), "checkpoint_load")
+
+    def output(self, root, index, time, dt, ascii=False):
+        self._ck(self._L.mhdgb_output(self._h, os.fsencode(root), index, time, dt, 1 if ascii else 0), "output")
 
     def init_kh(self, seed=1, vshear=0.5, width=0.05, bx=0.1, amp=1e-2, sig=0.2, noise=1e-4):
         self._ck(self._L.mhdgb_init_kh(self._h, seed, vshear, width, bx, amp, sig, noise), "init_kh")

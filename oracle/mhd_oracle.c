@@ -47,6 +47,7 @@ void orc_grid_init(orc_grid *g, int nx, int ny, int nz) {
   g->itot = nx + 2 * ORC_NGH + 1;
   g->jtot = ny + 2 * ORC_NGH + 1;
   g->ktot = nz + 2 * ORC_NGH + 1;
+  g->riemann = 0;
 }
 
 /* GenerateGrid, src_cpp_kokkos_host/main.cpp:35-44 (single rank: coords = 0, ntiles = 1). */
@@ -217,6 +218,62 @@ static void hlld(const double *leftst, const double *rigtst, double *nflux) {
   nflux[mbps] = 0.0; /* never read: the GLM pair overwrites it (mhd.cpp:1234-1237) */
 }
 
+/* HLLE, src_f90_acc_device/mhd.f90:877-907 (Fortran MIN/MAX written as std::min/std::max). */
+static void hlle(const double *leftst, const double *rigtst, double *nflux) {
+  const double csl = leftst[mcsp], csr = rigtst[mcsp];
+  const double vl = leftst[mvel], vr = rigtst[mvel];
+  double sl = SMIN(vl, vr) - SMAX(csl, csr);
+  sl = SMIN(0.0, sl);
+  double sr = SMAX(vl, vr) + SMAX(csl, csr);
+  sr = SMAX(0.0, sr);
+  for (int m = 0; m < mconsv; m++)
+    nflux[m] = (sr * leftst[mconsv + m] - sl * rigtst[mconsv + m] + sl * sr * (rigtst[m] - leftst[m])) / (sr - sl);
+}
+
+/* HLLC, src_f90_acc_device/mhd.f90:909-1141.  The Fortran routine reads sclst, the passive-scalar
+ * star state, without setting it; here it is scaled by rolst/rol like the transverse field. */
+static void hllc(const double *leftst, const double *rigtst, double *nflux) {
+  const double rol = leftst[mudn], eel = leftst[muet];
+  const double rxl = leftst[muvu], ryl = leftst[muvv], rzl = leftst[muvw];
+  const double vxl = leftst[muvu] / leftst[mudn], vyl = leftst[muvv] / leftst[mudn], vzl = leftst[muvw] / leftst[mudn];
+  const double scl = leftst[must], byl = leftst[mubv], bzl = leftst[mubw], ptl = leftst[mpre];
+  const double ror = rigtst[mudn], eer = rigtst[muet];
+  const double rxr = rigtst[muvu], ryr = rigtst[muvv], rzr = rigtst[muvw];
+  const double vxr = rigtst[muvu] / rigtst[mudn], vyr = rigtst[muvv] / rigtst[mudn], vzr = rigtst[muvw] / rigtst[mudn];
+  const double scr = rigtst[must], byr = rigtst[mubv], bzr = rigtst[mubw], ptr = rigtst[mpre];
+  const double cfl = leftst[mcsp], cfr = rigtst[mcsp];
+  const double sl = SMIN(vxl, vxr) - SMAX(cfl, cfr);
+  const double sr = SMAX(vxl, vxr) + SMAX(cfl, cfr);
+  const double sdl = sl - vxl, sdr = sr - vxr;
+  const double rosdl = rol * sdl, rosdr = ror * sdr;
+  const double temp = 1.0 / (rosdr - rosdl);
+  const double sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * temp;          /* eq. 45 */
+  const double sdml = sl - sm, isdml = 1.0 / sdml;
+  const double sdmr = sr - sm, isdmr = 1.0 / sdmr;
+  const double ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * temp;   /* eq. 49 */
+  const double rolst = rol * sdl * isdml;
+  const double rxlst = rolst * sm, rylst = rolst * vyl, rzlst = rolst * vzl;
+  const double bylst = rolst / rol * byl, bzlst = rolst / rol * bzl, sclst = rolst / rol * scl;
+  const double eelst = (sdl * eel - ptl * vxl + ptst * sm) * isdml;
+  const double rorst = rosdr * isdmr;
+  const double rxrst = rorst * sm, ryrst = rorst * vyr, rzrst = rorst * vzr;
+  const double byrst = rorst / ror * byr, bzrst = rorst / ror * bzr, scrst = rorst / ror * scr;
+  const double eerst = (sdr * eer - ptr * vxr + ptst * sm) * isdmr;
+  const double sign1 = copysign(1.0, sm);
+  const double maxs1 = SMAX(0.0, sign1), mins1 = -SMIN(0.0, sign1);
+  const double msl = SMIN(sl, 0.0), msr = SMAX(sr, 0.0);
+  nflux[mden] = (leftst[mfdn] + msl * (rolst - rol)) * maxs1 + (rigtst[mfdn] + msr * (rorst - ror)) * mins1;
+  nflux[meto] = (leftst[mfet] + msl * (eelst - eel)) * maxs1 + (rigtst[mfet] + msr * (eerst - eer)) * mins1;
+  nflux[mrvu] = (leftst[mfvu] + msl * (rxlst - rxl)) * maxs1 + (rigtst[mfvu] + msr * (rxrst - rxr)) * mins1;
+  nflux[mrvv] = (leftst[mfvv] + msl * (rylst - ryl)) * maxs1 + (rigtst[mfvv] + msr * (ryrst - ryr)) * mins1;
+  nflux[mrvw] = (leftst[mfvw] + msl * (rzlst - rzl)) * maxs1 + (rigtst[mfvw] + msr * (rzrst - rzr)) * mins1;
+  nflux[mbmu] = 0.0;
+  nflux[mbmv] = (leftst[mfbv] + msl * (bylst - byl)) * maxs1 + (rigtst[mfbv] + msr * (byrst - byr)) * mins1;
+  nflux[mbmw] = (leftst[mfbw] + msl * (bzlst - bzl)) * maxs1 + (rigtst[mfbw] + msr * (bzrst - bzr)) * mins1;
+  nflux[mbps] = 0.0;
+  nflux[mst] = (leftst[mfst] + msl * (sclst - scl)) * maxs1 + (rigtst[mfst] + msr * (scrst - scr)) * mins1;
+}
+
 /* Direction maps of Prim2Cons1/2/3, src_cpp_kokkos_host/mhd.cpp:1078-1118. */
 typedef struct dirmap {
   int muv1, muv2, muv3, mub1, mub2, mub3, mfv1, mfv2, mfv3, nved, nbmd, nvef, nbmf, nveb, nbmb;
@@ -264,7 +321,7 @@ static void prim2cons(const double *Prim, double *Cons, const dirmap *d) {
 
 /* CalcFlux, src_cpp_kokkos_host/mhd.cpp:1120-1158 */
 static void calc_flux(const double *L1, const double *L2, const double *R1, const double *R2,
-                      double *numflux, double *Cl, double *Cr, const dirmap *d) {
+                      double *numflux, double *Cl, double *Cr, const dirmap *d, int riemann) {
   double Pl[nprim], Pr[nprim];
   for (int n = 0; n < nprim; n++) {
     double dsvp = R1[n] - L2[n];
@@ -278,7 +335,9 @@ static void calc_flux(const double *L1, const double *L2, const double *R1, cons
     Pr[n] = R1[n] - 0.5e0 * van_leer(dsvp, dsvm);
   }
   prim2cons(Pr, Cr, d);
-  hlld(Cl, Cr, numflux);
+  if (riemann == 1) hlle(Cl, Cr, numflux);
+  else if (riemann == 2) hllc(Cl, Cr, numflux);
+  else hlld(Cl, Cr, numflux);
 }
 
 /* GetNumericalFluxD, src_cpp_kokkos_host/mhd.cpp:987-1410 (Flux1 1204-1241, Flux2 1287-1322,
@@ -312,7 +371,7 @@ void orc_flux(int dir, const orc_grid *g, const double *P, double *F, double chg
           R1[n] = P[ix(g, nprim, n, k, j, i)];
           R2[n] = P[ix(g, nprim, n, k + dk, j + dj, i + di)];
         }
-        calc_flux(L1, L2, R1, R2, nf, Cl, Cr, d);
+        calc_flux(L1, L2, R1, R2, nf, Cl, Cr, d, g->riemann);
         F[ix(g, mconsv, mden, k, j, i)] = nf[mden];
         F[ix(g, mconsv, mrv1, k, j, i)] = nf[map_rv1];
         F[ix(g, mconsv, mrv2, k, j, i)] = nf[map_rv2];

@@ -30,6 +30,7 @@ typedef struct orc_grid {
   int bc[6];               /* xin, xout, yin, yout, zin, zout (1 periodic, 2 reflection, 3 outflow) */
   int spacing_quirk;       /* 1: UpdateConservU takes y/z spacings at index i, as mhd.cpp:1435-1436 */
   const double *x1a, *x2a, *x3a;  /* cell-face coordinates, length itot / jtot / ktot */
+  int riemann;             /* 0 HLLD (mhd.cpp:97-417), 1 HLLE, 2 HLLC (src_f90_acc_device/mhd.f90:877-1141) */
 } orc_grid;
 
 /* Fill extents from nx,ny,nz (call before use). */

@@ -24,6 +24,7 @@ class OrcGrid(C.Structure):
         ("gam", C.c_double), ("cfl", C.c_double),
         ("bc", C.c_int * 6), ("spacing_quirk", C.c_int),
         ("x1a", C.POINTER(C.c_double)), ("x2a", C.POINTER(C.c_double)), ("x3a", C.POINTER(C.c_double)),
+        ("riemann", C.c_int),
     ]
 
 
@@ -69,7 +70,7 @@ class Oracle:
     """One grid configuration of the oracle; methods mirror the reference stage functions."""
 
     def __init__(self, nx, ny, nz, x1a, x2a, x3a, gam=5.0 / 3.0, cfl=0.05, bc=(1, 1, 2, 2, 1, 1),
-                 spacing_quirk=True):
+                 spacing_quirk=True, riemann=0):
         self.axes = [np.ascontiguousarray(a, dtype=np.float64) for a in (x1a, x2a, x3a)]
         g = OrcGrid()
         g.nx, g.ny, g.nz = nx, ny, nz
@@ -77,6 +78,7 @@ class Oracle:
         g.gam, g.cfl = gam, cfl
         g.bc = (C.c_int * 6)(*bc)
         g.spacing_quirk = 1 if spacing_quirk else 0
+        g.riemann = riemann  # 0 HLLD, 1 HLLE, 2 HLLC
         g.x1a, g.x2a, g.x3a = (_ptr(a) for a in self.axes)
         self.g = g
         self.shape = (g.ktot, g.jtot, 0, g.itot)

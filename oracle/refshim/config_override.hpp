@@ -41,7 +41,10 @@ inline constexpr int boundary_yin = reflection;
 inline constexpr int boundary_yout = reflection;
 inline constexpr int boundary_zin = periodicb;
 inline constexpr int boundary_zout = periodicb;
-inline constexpr bool asciiout = false;
+#ifndef REF_ASCIIOUT
+#define REF_ASCIIOUT false
+#endif
+inline constexpr bool asciiout = REF_ASCIIOUT;
 inline constexpr bool benchmarkmode = true;
 };  // namespace config
 

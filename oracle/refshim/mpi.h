@@ -62,4 +62,46 @@ static inline int MPI_Isend(const void *, size_t, MPI_Datatype, int, int, MPI_Co
 }
 static inline int MPI_Waitall(int, MPI_Request *, MPI_Status *) { return 0; }
 
+/* MPI-IO as src_cpp_kokkos_host/output.cpp uses it, for one rank: every subarray view covers the
+ * whole file (sizes == subsizes, starts == 0, checked), so a collective write is a plain write at
+ * the view's displacement.  MPI_File_open does not truncate, as MPI does not. */
+typedef long long MPI_Offset;
+typedef int MPI_Info;
+typedef FILE *MPI_File;
+#define MPI_INFO_NULL 0
+#define MPI_DATATYPE_NULL 0
+#define MPI_STATUS_IGNORE ((MPI_Status *)0)
+#define MPI_ORDER_C 56
+#define MPI_MODE_CREATE 1
+#define MPI_MODE_WRONLY 4
+
+static inline int MPI_Type_create_subarray(int ndims, const int *sizes, const int *subsizes, const int *starts, int,
+                                           MPI_Datatype, MPI_Datatype *newtype) {
+  for (int d = 0; d < ndims; d++)
+    if (sizes[d] != subsizes[d] || starts[d] != 0) {
+      fprintf(stderr, "refshim: a one-rank subarray must cover the whole array\n");
+      abort();
+    }
+  *newtype = 100 + ndims;
+  return 0;
+}
+static inline int MPI_Type_commit(MPI_Datatype *) { return 0; }
+static inline int MPI_File_open(MPI_Comm, const char *name, int, MPI_Info, MPI_File *fh) {
+  *fh = fopen(name, "r+b");
+  if (!*fh) *fh = fopen(name, "w+b");
+  return *fh ? 0 : 1;
+}
+static inline int MPI_File_set_view(MPI_File fh, MPI_Offset disp, MPI_Datatype, MPI_Datatype, const char *, MPI_Info) {
+  return fh && fseek(fh, (long)disp, SEEK_SET) == 0 ? 0 : 1;
+}
+static inline int MPI_File_write_all(MPI_File fh, const void *buf, MPI_Offset count, MPI_Datatype t, MPI_Status *) {
+  const size_t sz = t == MPI_DOUBLE ? sizeof(double) : sizeof(int);
+  return fh && fwrite(buf, sz, (size_t)count, fh) == (size_t)count ? 0 : 1;
+}
+static inline int MPI_File_close(MPI_File *fh) {
+  if (*fh) fclose(*fh);
+  *fh = 0;
+  return 0;
+}
+
 #endif

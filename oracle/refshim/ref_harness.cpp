@@ -18,6 +18,7 @@
 #include "config.hpp"
 #include "mhd.hpp"
 #include "mpi_config.hpp"
+#include "ref_grid.hpp"
 
 using namespace resolution_mod;
 using namespace hydflux_mod;
@@ -29,19 +30,6 @@ static void fail(const char* m) {
 
 static void dump(FILE* f, const FieldArray<double>& A) {
   if (std::fwrite(A.data, sizeof(double), A.size, f) != A.size) fail("short write");
-}
-
-static void setup_grid(GridArray<double>& G) {
-  // single-rank form of main.cpp:35-64 (coords = 0, ntiles = 1), same operations
-  const double x1minloc = x1min + (x1max - x1min) / 1 * 0, x1maxloc = x1min + (x1max - x1min) / 1 * (0 + 1);
-  const double dx1 = (x1maxloc - x1minloc) / double(ngrid1);
-  for (int i = is - ngh; i <= ie + ngh + 1; i++) G.x1a(i) = dx1 * (i - (ngh + 1)) + x1minloc;
-  const double x2minloc = x2min + (x2max - x2min) / 1 * 0, x2maxloc = x2min + (x2max - x2min) / 1 * (0 + 1);
-  const double dx2 = (x2maxloc - x2minloc) / double(ngrid2);
-  for (int j = js - ngh; j <= je + ngh + 1; j++) G.x2a(j) = dx2 * (j - (ngh + 1)) + x2minloc;
-  const double x3minloc = x3min + (x3max - x3min) / 1 * 0, x3maxloc = x3min + (x3max - x3min) / 1 * (0 + 1);
-  const double dx3 = (x3maxloc - x3minloc) / double(ngrid3);
-  for (int k = ks - ngh; k <= ke + ngh + 1; k++) G.x3a(k) = dx3 * (k - (ngh + 1)) + x3minloc;
 }
 
 int main(int argc, char** argv) {
@@ -60,7 +48,7 @@ int main(int argc, char** argv) {
   mpi_config_mod::InitializeMPI();
   AllocateHydroVariables(G, U, Fx, Fy, Fz, P);
   boundary_mod::AllocateBoundaryVariables(boundary_mod::Bs, boundary_mod::Br);
-  setup_grid(G);
+  ref_setup_grid(G);
   gam = g;
   boundary_mod::boundary_xin = bc[0];
   boundary_mod::boundary_xout = bc[1];

@@ -1,4 +1,5 @@
-"""Generate the golden vectors in this folder by running the reference's own solver stages.
+"""Generate the golden vectors in this folder by running the reference's own solver stages and its
+own output routine.
 
 The reference's src_cpp_kokkos_host/{mhd,boundary,mpi_config}.cpp are compiled unmodified from the
 reference tree against oracle/refshim/ (``make -C oracle ref``), driven by oracle/refshim/ref_harness.cpp
@@ -6,12 +7,17 @@ in the stage order of src_cpp_kokkos_host/main.cpp:229-259, and their outputs ar
 compressed .npz files.  Needs the reference tree (only present where the fixtures are made);
 the tests only read the .npz files.
 
-    python tests/golden/make_golden.py [--refdir /path/to/src_cpp_kokkos_host]
+    python tests/golden/make_golden.py [--refdir /path/to/src_cpp_kokkos_host] [--only stages|output]
 
 Each case stores:  meta (nx,ny,nz,gam,bc,nsteps,domain), U0 (input conserved state; only the
 interior is meaningful), dts/chgs (per step), and interior or full arrays P0 (UpdatePrimitvP of
 the input), P1/U1 (after step 1), PN/UN (after nsteps), F1 (the three face-flux arrays of step 1,
 full cases only).
+
+The output case (output_7x5x4.npz) runs the reference's Output() (src_cpp_kokkos_host/output.cpp,
+``make -C oracle refout``, driven by oracle/refshim/ref_output.cpp) on two primitive states and
+stores: meta (nx,ny,nz), domain, td (time, dt per snapshot), P (the full input arrays) and every
+file it wrote (names: relative paths, blob_<i>: the bytes).
 """
 from __future__ import annotations
 
@@ -94,10 +100,44 @@ def run_ref(exe, n, U0, bc, nsteps, dump_flux):
     return out
 
 
+OUTPUT_CASE = ("output_7x5x4", (7, 5, 4), ic.KH_DOMAIN, [(0.0, 0.0), (0.12345678901234567, 1.5e-3)])
+
+
+def make_output_golden(refdir):
+    name, (nx, ny, nz), domain, td = OUTPUT_CASE
+    subprocess.run(["make", "-s", "-B", "-C", os.path.join(ROOT, "oracle"), "refout", f"NX={nx}", f"NY={ny}",
+                    f"NZ={nz}", f"REFDIR={refdir}", f"DOMAIN={domain_flags(domain)}"], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", f"refout_{nx}x{ny}x{nz}")
+    it, jt, kt = ic.extents(nx, ny, nz)
+    rng = np.random.default_rng(77)
+    Ps = np.stack([rng.uniform(0.5, 2.0, (kt, jt, 12, it)), rng.standard_normal((kt, jt, 12, it))])
+    with tempfile.TemporaryDirectory() as tdir:
+        fin = os.path.join(tdir, "in.bin")
+        with open(fin, "wb") as f:
+            np.array([nx, ny, nz, len(td)], dtype="<i4").tofile(f)
+            for (t, dt), P in zip(td, Ps):
+                np.array([t, dt], dtype="<f8").tofile(f)
+                P.astype("<f8").tofile(f)
+        subprocess.run([exe, fin], check=True, cwd=tdir, stdout=subprocess.DEVNULL)
+        names = sorted(os.path.relpath(os.path.join(d, fn), tdir) for d, _, fs in os.walk(tdir) for fn in fs
+                       if fn != "in.bin")
+        blobs = {f"blob_{i}": np.frombuffer(open(os.path.join(tdir, nm), "rb").read(), dtype=np.uint8)
+                 for i, nm in enumerate(names)}
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, meta=np.array([nx, ny, nz]), domain=np.array(domain, dtype=np.float64),
+                        td=np.array(td, dtype=np.float64), P=Ps, names=np.array(names), **blobs)
+    print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, files: {' '.join(names)}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--refdir", default="/root/reference/src_cpp_kokkos_host")
+    ap.add_argument("--only", choices=["stages", "output"], default=None)
     args = ap.parse_args()
+    if args.only != "stages":
+        make_output_golden(args.refdir)
+    if args.only == "output":
+        return
     for name, n, builder, domain, bc, nsteps, full in CASES:
         exe = build_ref(n, domain, args.refdir, name)
         U0 = ic.prim_to_cons(builder(n), GAM)

@@ -35,4 +35,6 @@ class Case:
 
 
 def cases():
-    return [Case(p) for p in sorted(glob.glob(os.path.join(HERE, "*.npz")))]
+    """The stage cases (every .npz but the output case output_*.npz)."""
+    paths = sorted(glob.glob(os.path.join(HERE, "*.npz")))
+    return [Case(p) for p in paths if not os.path.basename(p).startswith("output_")]

@@ -24,7 +24,7 @@ inline constexpr int boundary_yin = reflection;
 inline constexpr int boundary_yout = reflection;
 inline constexpr int boundary_zin = periodicb;
 inline constexpr int boundary_zout = periodicb;
-inline constexpr bool asciiout = false;
+inline constexpr bool asciiout = true;
 inline constexpr bool benchmarkmode = true;
 };  // namespace config
 namespace resolution_mod {
@@ -33,6 +33,7 @@ inline double time_sim = 0.0e0;
 inline double time_out = 0.0e0;
 inline double dt;
 inline constexpr double time_max = config::time_max;
+inline constexpr double dtout = config::dtout;
 inline constexpr int ngrid1 = config::ngridtotal1 / config::ntiles[0];
 inline constexpr int ngrid2 = config::ngridtotal2 / config::ntiles[1];
 inline constexpr int ngrid3 = config::ngridtotal3 / config::ntiles[2];

@@ -1,10 +1,12 @@
 // A program in the shape of the reference's src_cpp_kokkos_device/main.cpp, written against the
 // drop-in header include/mhdgb_ref_api.hpp: grid, a KH state set in P and U on the host, h2d, the
-// stage loop of main.cpp:317-351, d2h.  Writes the initial P, U and the final U, P, dt, chg to the
-// file named by argv[1] (read by tests/test_gpu_refapi.py).
+// stage loop of main.cpp:317-351, d2h, and the forced snapshot outputs of main.cpp:219 and 279.
+// Writes the initial P, U and the final U, P, dt, chg to the file named by argv[1] (read by
+// tests/test_gpu_refapi.py); the snapshots go to bindata/ and ascdata/ in the working directory.
 #include <cmath>
 #include <cstdio>
 
+#define MHDGB_REF_OUTPUT  // the header's Output() stands in for output.cpp's
 #include "mhdgb_ref_api.hpp"
 
 using namespace resolution_mod;
@@ -64,6 +66,7 @@ int main(int argc, char** argv) {
   G.h2d();
   P.h2d();
   U.h2d();
+  Output(true);
   std::vector<double> dts, chgs;
   for (int step = 0; step < nsteps; step++) {
     ControlTimestep(G, P);
@@ -79,6 +82,7 @@ int main(int argc, char** argv) {
     dts.push_back(dt);
     chgs.push_back(chg);
   }
+  Output(true);
   U.d2h();
   P.d2h();
   write(f, U);
