@@ -176,8 +176,14 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   // Step 5A (mhd.cpp:269-300)
   const R bxs = R(0.5) * (leftst[mubu] + rigtst[mubu]);
   const R bxsq = bxs * bxs;
+  // Degenerate star states (rho (S - v)(S - S_M) = B_x^2, e.g. field-aligned flow with c_f = v_A):
+  // the reference switches to v* = v, B* = B below |T| < 1e-30, which FP64 rounding noise (~1e-16)
+  // never reaches.  In FP32 both T and the numerators it divides are rounding noise (~1e-7) there,
+  // so the FP32 solver treats |T| < 3e-4 p_T* (about the square root of FP32's epsilon, relative
+  // to the star total pressure) as degenerate; faces with B_n ~ 0 have T ~ rho c_f^2, far above.
+  const R deg = std::is_same<R, float>::value ? smax(eps, R(3e-4) * fabs(ptst)) : eps;
   R temp_fst = rosdl * sdml - bxsq;
-  R sign1 = copysign(R(1), fabs(temp_fst) - eps);
+  R sign1 = copysign(R(1), fabs(temp_fst) - deg);
   R maxs1 = smax(R(0), sign1);
   R mins1 = smin(R(0), sign1);
   R itf = fdiv(R(1), temp_fst + mins1);
@@ -199,7 +205,7 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
                   - mins1 * eel;
   // Step 5B (mhd.cpp:305-333)
   temp_fst = rosdr * sdmr - bxsq;
-  sign1 = copysign(R(1), fabs(temp_fst) - eps);
+  sign1 = copysign(R(1), fabs(temp_fst) - deg);
   maxs1 = smax(R(0), sign1);
   mins1 = smin(R(0), sign1);
   itf = fdiv(R(1), temp_fst + mins1);
