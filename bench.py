@@ -322,7 +322,14 @@ def run_ours(args, ws, rank, local):
     if prof and prof.get("dp_flops_per_cell") and fp64_rate:
         ach = prof["dp_flops_per_cell"] * cells / (ms_step * 1e-3) / 1e9
         fp64_pipe = {"achieved": ach, "peak": fp64_rate, "unit": "GFLOP/s", "frac": ach / fp64_rate,
-                     "peak_kind": "measured (DFMA probe, mhdgb_measure_fp64_rate)"}
+                     "peak_kind": "measured (DFMA probe, mhdgb_measure_fp64_rate)",
+                     "flops_per_cell": prof["dp_flops_per_cell"]}
+        if prof.get("fp64_pipe_inst_per_cell"):
+            # issue fraction: all FP64-pipe instructions (compares and selects included) against the
+            # probe's DFMA issue rate (fp64_rate / 2 instructions per second)
+            inst = prof["fp64_pipe_inst_per_cell"] * cells / (ms_step * 1e-3) / 1e9
+            fp64_pipe["inst_frac"] = inst / (fp64_rate / 2.0)
+            fp64_pipe["pipe_active_ncu"] = prof.get("fp64_pipe_active_ncu")
     mx = res["mixed"]
     mx_step = mx["ms"] / mx["steps"]
     mx_value = replica_value(ws, cells, mx["steps"], mx["ms"])

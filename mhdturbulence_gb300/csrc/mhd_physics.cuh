@@ -62,7 +62,12 @@ __device__ __forceinline__ R fdiv(R a, R b) {
 // per cell and direction gives both.
 template <class R>
 __device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
-  return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
+  if constexpr (kFast) {  // one product for the test and the numerator: p + p == (2 dsvp) dsvm exactly
+    const R p = dsvp * dsvm;
+    return (p > R(0)) ? fdiv(p + p, dsvp + dsvm) : R(0);
+  } else {
+    return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
+  }
 }
 
 // Rotation maps of Prim2Cons1/2/3, mhd.cpp:1078-1118.
