@@ -385,10 +385,11 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     const int pxs = (nxs + 31) & ~31, pys = (nys + 31) & ~31, pzs = (nzs + 31) & ~31;
     const int pxf = (nxf + 31) & ~31, pyf = (nyf + 31) & ~31, pzf = (nzf + 31) & ~31;
 
+    // Two barriers per plane.  Phase A writes only slope buffers that the previous plane's phase C
+    // does not read, and phase C reads no ring plane, so neither the start nor the end of a plane
+    // needs a barrier; the ring slot of plane k is reloaded once phase B has read it.
     for (int k = kb; k < ke; k++) {
       wait_plane(k + 2);
-      __syncthreads();
-      if (s_abort) break;
       const R *pk = plane(k), *pk1 = plane(k + 1), *pk2 = plane(k + 2);
       // ---- phase A: slopes ----
       for (int q = tid; q < pxs + pys + pzs; q += NT) {
@@ -424,6 +425,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         }
       }
       __syncthreads();
+      if (s_abort) break;  // a plane that never arrived (bounded wait): the data above is not used
       // ---- phase B: face fluxes (on the first plane also the faces kb-1/2, into slope buffer 2) ----
       const int nq = pxf + pyf + (k == kb ? 2 * pzf : pzf);
       for (int q = tid; q < nq; q += NT) {
@@ -477,7 +479,21 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
           }
         }
       }
-      __syncthreads();
+      __syncthreads();  // faces formed; plane k (and on the first plane kb-1) read for the last time
+      if (k == kb && kb + 3 <= ke + 1) {  // plane kb-1's slot
+        if (tid == 0) {
+          fence_proxy_async();
+          issue(kb + 3);
+        }
+        fills[slot_of(kb + 3)]++;
+      }
+      if (k + 4 <= ke + 1) {  // plane k's slot
+        if (tid == 0) {
+          fence_proxy_async();
+          issue(k + 4);
+        }
+        fills[slot_of(k + 4)]++;
+      }
       // ---- phase C: cell update, recovery, ghost images, candidates ----
       if (own) {
         if (k == kb) {
@@ -506,21 +522,6 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
                         spacing_of<R>(a, 1, jj + NGH), spacing_of<R>(a, 2, k + NGH), dtc, chc, bad);
         cmin = smin(cmin, dtc);
         cmax = smax(cmax, chc);
-      }
-      __syncthreads();  // plane k and the work buffers retired
-      if (k == kb && kb + 3 <= ke + 1) {  // plane kb-1's slot is free now
-        if (tid == 0) {
-          fence_proxy_async();
-          issue(kb + 3);
-        }
-        fills[slot_of(kb + 3)]++;
-      }
-      if (k + 4 <= ke + 1) {
-        if (tid == 0) {
-          fence_proxy_async();
-          issue(k + 4);
-        }
-        fills[slot_of(k + 4)]++;
       }
       zb ^= 1;
     }
