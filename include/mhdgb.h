@@ -187,9 +187,10 @@ int mhdgb_autotune(mhdgb_solver* h, int steps, int* best);
  * FP64-pipe roofline of the FP64 form, which is bound by FP64 issue rather than by HBM. */
 int mhdgb_measure_fp64_rate(int device, double* gflops);
 
-/* Self-test of the FP64 division used by the FMA-contracted FP64 form (FP32-seeded reciprocal with
- * two Newton-Raphson steps) against IEEE division on n random operand pairs; *max_ulp receives
- * the largest difference in units in the last place. */
+/* Self-test of the FP64 division and square root used by the FMA-contracted FP64 form (FP32-seeded
+ * reciprocal with two Newton-Raphson steps; FP32-seeded Goldschmidt square root and reciprocal
+ * square root) against IEEE division and square root on n random operands; *max_ulp receives the
+ * largest difference in units in the last place. */
 int mhdgb_selftest_division(int device, int n, unsigned long long seed, double* max_ulp);
 
 /* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):

@@ -8,8 +8,9 @@
 namespace mhdgb {
 namespace {
 
-// The FP64 division of the fast build against IEEE division on log-uniform operands of both signs
-// over [2^-60, 2^60]: the largest distance in units in the last place.
+// The FP64 division, square root and reciprocal square root of the fast build against IEEE
+// division and square root on log-uniform operands (both signs for the division) over
+// [2^-60, 2^60]: the largest distance in units in the last place.
 __global__ void k_fdiv_selftest(int n, unsigned long long seed, unsigned long long* max_ulp) {
   unsigned long long worst = 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -26,6 +27,16 @@ __global__ void k_fdiv_selftest(int n, unsigned long long seed, unsigned long lo
     const long long d = (long long)__double_as_longlong(q) - (long long)__double_as_longlong(r);
     const unsigned long long ad = (unsigned long long)(d < 0 ? -d : d);
     if (ad > worst) worst = ad;
+    // the square root of the fast form (and the reciprocal square root it also yields)
+    const double x = fabs(a);
+    double ix = 0.0;
+    const double sq = v_fast64::sqrt_goldschmidt(x, &ix), sr = sqrt(x), ir = 1.0 / sr;
+    const long long ds = (long long)__double_as_longlong(sq) - (long long)__double_as_longlong(sr);
+    const long long di = (long long)__double_as_longlong(ix) - (long long)__double_as_longlong(ir);
+    const unsigned long long ads = (unsigned long long)(ds < 0 ? -ds : ds);
+    const unsigned long long adi = (unsigned long long)(di < 0 ? -di : di);
+    if (ads > worst) worst = ads;
+    if (adi > worst) worst = adi;
   }
   atomicMax(max_ulp, worst);
 }

@@ -43,6 +43,43 @@ __device__ __forceinline__ double rcp_newton(double b) {
   return r;
 }
 
+// FP64 square root by Goldschmidt's iteration from an FP32 reciprocal-square-root seed y (MUFU,
+// error ~2^-22): g = x y ~ sqrt(x) and h = y/2 ~ 1/(2 sqrt(x)) are refined together by
+// r = 1/2 - g h, g += g r, h += h r (error ~2^-44), then one Newton correction of g with the
+// residual x - g^2 (formed by an FMA): g += h (x - g^2).  Seven FP64 operations against nine for
+// the IEEE routine; arguments outside [2^-120, 2^120] (zero, denormals, negatives, inf, NaN) take
+// the IEEE square root.  Given inv, *inv receives 1/sqrt(x) from a second correction of h.
+__device__ __forceinline__ bool sqrt_seed_range(double x) {
+  const unsigned e = (unsigned)__double2hiint(x) >> 20;  // the sign bit makes negatives fail
+  return e >= 1023u - 120u && e <= 1023u + 120u;
+}
+__device__ __forceinline__ double sqrt_goldschmidt(double x, double* inv = nullptr) {
+  float yf;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(d2f_rne(x)));
+  const double y = f2d_exact(yf);
+  double g = x * y, h = 0.5 * y;
+  const double r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  const double d = fma(-g, g, x);
+  if (inv) {
+    const double r2 = fma(-g, h, 0.5);
+    const double hh = fma(h, r2, h);
+    *inv = hh + hh;
+  }
+  return fma(d, h, g);
+}
+
+// sqrt: IEEE in the exact build and in FP32; sqrt_goldschmidt in the FP64 fast build.
+template <class R>
+__device__ __forceinline__ R fsqrt(R x) {
+  if constexpr (kFast && std::is_same<R, double>::value) {
+    return sqrt_seed_range(x) ? sqrt_goldschmidt(x) : sqrt(x);
+  } else {
+    return sqrt(x);
+  }
+}
+
 // a / b: IEEE division in the exact build and in FP32; a * rcp_newton(b) in the FP64 fast build
 // (within ~1.5 ulp), with IEEE division where |b| is outside the FP32 seed's range.
 template <class R>
@@ -129,7 +166,7 @@ __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC
   Cons[mfst] = rho * Prim[nst] * Prim[D::nved];
   const R css = Prim[ncsp] * Prim[ncsp];
   const R cts = css + bsq * rhoinv;
-  Cons[mcsp] = sqrt((cts + sqrt(cts * cts - R(4) * css * Prim[D::nbmd] * Prim[D::nbmd] * rhoinv)) / R(2));
+  Cons[mcsp] = fsqrt((cts + fsqrt(cts * cts - R(4) * css * Prim[D::nbmd] * Prim[D::nbmd] * rhoinv)) / R(2));
   Cons[mvel] = Prim[D::nved];
   Cons[mpre] = ptl;
 }
@@ -364,7 +401,15 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   R vydst = vyst, vzdst = vzst, bydst = byst, bzdst = bzst, eedst = eest, sst = R(0);
   if (!(abbx - eps < R(0))) {
     const R signbx = copysign(R(1), bxs);
-    const R sq = sqrt(rost), so_sq = sqrt(so_rost);
+    // sqrt of the upwind star density and its reciprocal from one Goldschmidt iteration
+    R sq, isq;
+    if (sqrt_seed_range(rost)) {
+      sq = sqrt_goldschmidt(rost, &isq);
+    } else {
+      sq = sqrt(rost);
+      isq = R(1) / sq;
+    }
+    const R so_sq = fsqrt(so_rost);
     // (sqrtrol, sqrtror) ordered as in the reference
     const R sql = left ? sq : so_sq, sqr = left ? so_sq : sq;
     const R invsumro = fdiv(R(1), sql + sqr);
@@ -379,7 +424,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
     const R vdbst = vxst * bxs + vyst * byst + vzst * bzst;
     const R tdd = sm * bxs + vydst * bydst + vzdst * bzdst;
     eedst = left ? eest - sq * signbx * (vdbst - tdd) : eest + sq * signbx * (vdbst - tdd);
-    sst = left ? sm - fdiv(abbx, sq) : sm + fdiv(abbx, sq);
+    sst = left ? sm - abbx * isq : sm + abbx * isq;
   }
   // Step 6: flux of the upwind side
   const R ms = left ? smin(s_, R(0)) : smax(s_, R(0));
@@ -529,7 +574,7 @@ __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPR
   const R emag = R(0.5) * (u[mbm1] * u[mbm1] + u[mbm2] * u[mbm2] + u[mbm3] * u[mbm3]);
   p[nene] = kFast ? (u[meto] - ekin - emag) * rhoinv : (u[meto] - ekin - emag) / u[mden];
   p[npre] = p[nene] * p[nden] * (gam - R(1));
-  p[ncsp] = sqrt(p[nene] * gam * (gam - R(1)));
+  p[ncsp] = fsqrt(p[nene] * gam * (gam - R(1)));
   p[nbm1] = u[mbm1];
   p[nbm2] = u[mbm2];
   p[nbm3] = u[mbm3];
@@ -540,7 +585,7 @@ __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPR
 // Per-cell CFL time (ControlTimestep, mhd.cpp:1542-1550): min over d of dx_d/(|v_d| + ctot).
 template <class R>
 __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
-  const R ctot = sqrt(p[ncsp] * p[ncsp] + fdiv(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
+  const R ctot = fsqrt(p[ncsp] * p[ncsp] + fdiv(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
   R dt = fdiv(dx, fabs(p[nve1]) + ctot);
   const R b = fdiv(dy, fabs(p[nve2]) + ctot);
   const R c = fdiv(dz, fabs(p[nve3]) + ctot);
@@ -558,11 +603,11 @@ __device__ __forceinline__ R cell_ch(const R (&p)[NPRIM]) {
   const R ca2 = kFast ? p[nbm2] * p[nbm2] * ri : p[nbm2] * p[nbm2] / p[nden];
   const R ca3 = kFast ? p[nbm3] * p[nbm3] * ri : p[nbm3] * p[nbm3] / p[nden];
   const R cts = css + ca1 + ca2 + ca3;
-  const R cm1 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca1)) / R(2));
+  const R cm1 = fsqrt((cts + fsqrt(cts * cts - R(4) * css * ca1)) / R(2));
   const R ch1 = (fabs(p[nve1]) + cm1);
-  const R cm2 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca2)) / R(2));
+  const R cm2 = fsqrt((cts + fsqrt(cts * cts - R(4) * css * ca2)) / R(2));
   const R ch2 = (fabs(p[nve2]) + cm2);
-  const R cm3 = sqrt((cts + sqrt(cts * cts - R(4) * css * ca3)) / R(2));
+  const R cm3 = fsqrt((cts + fsqrt(cts * cts - R(4) * css * ca3)) / R(2));
   const R ch3 = (fabs(p[nve3]) + cm3);
   R m = ch1;
   if (m < ch2) m = ch2;
