@@ -93,6 +93,24 @@ __device__ __forceinline__ R fdiv(R a, R b) {
   }
 }
 
+// a / b for quantities that only limit or estimate (slopes, wave-speed estimates, the dt and c_h
+// candidates): in the FP64 fast build one Newton step from the FP32 seed (relative error ~2^-44;
+// these values reach the state only as a small relative perturbation of a small quantity, ~1e-15
+// after a step); fdiv otherwise.
+template <class R>
+__device__ __forceinline__ R fdiv_est(R a, R b) {
+  if constexpr (kFast && std::is_same<R, double>::value) {
+    const unsigned e = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
+    if (e < 1023u - 120u || e > 1023u + 120u) return a / b;
+    float sf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(d2f_rne(b)));
+    const double r = f2d_exact(sf);
+    return a * fma(r, fma(-b, r, 1.0), r);
+  } else {
+    return fdiv(a, b);
+  }
+}
+
 // vanLeer, src_cpp_kokkos_host/mhd.cpp:89-95.  The limited slope of a cell c is
 // van_leer(P[c+1]-P[c], P[c]-P[c-1]); the reference evaluates the same expression for the left
 // state of face c+1/2 and the right state of face c-1/2 (mhd.cpp:1134-1154), so one evaluation
@@ -101,7 +119,7 @@ template <class R>
 __device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
   if constexpr (kFast) {  // one product for the test and the numerator: p + p == (2 dsvp) dsvm exactly
     const R p = dsvp * dsvm;
-    return (p > R(0)) ? fdiv(p + p, dsvp + dsvm) : R(0);
+    return (p > R(0)) ? fdiv_est(p + p, dsvp + dsvm) : R(0);
   } else {
     return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
   }
@@ -139,7 +157,7 @@ template <class R, int DIR>
 __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
   using D = Dir<DIR>;
   const R rho = Prim[nden];
-  const R rhoinv = fdiv(R(1), rho);
+  const R rhoinv = fdiv_est(R(1), rho);  // only in the fast-speed estimate below
   const R vsq = Prim[nve1] * Prim[nve1] + Prim[nve2] * Prim[nve2] + Prim[nve3] * Prim[nve3];
   const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
   Cons[mudn] = rho;
@@ -585,10 +603,10 @@ __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPR
 // Per-cell CFL time (ControlTimestep, mhd.cpp:1542-1550): min over d of dx_d/(|v_d| + ctot).
 template <class R>
 __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
-  const R ctot = fsqrt(p[ncsp] * p[ncsp] + fdiv(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
-  R dt = fdiv(dx, fabs(p[nve1]) + ctot);
-  const R b = fdiv(dy, fabs(p[nve2]) + ctot);
-  const R c = fdiv(dz, fabs(p[nve3]) + ctot);
+  const R ctot = fsqrt(p[ncsp] * p[ncsp] + fdiv_est(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
+  R dt = fdiv_est(dx, fabs(p[nve1]) + ctot);
+  const R b = fdiv_est(dy, fabs(p[nve2]) + ctot);
+  const R c = fdiv_est(dz, fabs(p[nve3]) + ctot);
   if (b < dt) dt = b;
   if (c < dt) dt = c;
   return dt;
@@ -598,7 +616,7 @@ __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
 template <class R>
 __device__ __forceinline__ R cell_ch(const R (&p)[NPRIM]) {
   const R css = p[ncsp] * p[ncsp];
-  const R ri = kFast ? fdiv(R(1), p[nden]) : R(0);  // fast form: one reciprocal of rho
+  const R ri = kFast ? fdiv_est(R(1), p[nden]) : R(0);  // fast form: one reciprocal of rho
   const R ca1 = kFast ? p[nbm1] * p[nbm1] * ri : p[nbm1] * p[nbm1] / p[nden];
   const R ca2 = kFast ? p[nbm2] * p[nbm2] * ri : p[nbm2] * p[nbm2] / p[nden];
   const R ca3 = kFast ? p[nbm3] * p[nbm3] * ri : p[nbm3] * p[nbm3] / p[nden];
