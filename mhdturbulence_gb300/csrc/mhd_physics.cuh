@@ -80,6 +80,23 @@ __device__ __forceinline__ R fsqrt(R x) {
   }
 }
 
+// sqrt of quantities that only estimate wave speeds (sound and fast speeds, the dt and c_h
+// candidates): in the FP64 fast build one Goldschmidt iteration without the final correction
+// (relative error ~2^-44, four FP64 operations); sqrt otherwise.
+template <class R>
+__device__ __forceinline__ R fsqrt_est(R x) {
+  if constexpr (kFast && std::is_same<R, double>::value) {
+    if (!sqrt_seed_range(x)) return sqrt(x);
+    float yf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(d2f_rne(x)));
+    const double y = f2d_exact(yf);
+    const double g = x * y;
+    return fma(g, fma(-g, 0.5 * y, 0.5), g);
+  } else {
+    return sqrt(x);
+  }
+}
+
 // a / b: IEEE division in the exact build and in FP32; a * rcp_newton(b) in the FP64 fast build
 // (within ~1.5 ulp), with IEEE division where |b| is outside the FP32 seed's range.
 template <class R>
@@ -184,7 +201,7 @@ __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC
   Cons[mfst] = rho * Prim[nst] * Prim[D::nved];
   const R css = Prim[ncsp] * Prim[ncsp];
   const R cts = css + bsq * rhoinv;
-  Cons[mcsp] = fsqrt((cts + fsqrt(cts * cts - R(4) * css * Prim[D::nbmd] * Prim[D::nbmd] * rhoinv)) / R(2));
+  Cons[mcsp] = fsqrt_est((cts + fsqrt_est(cts * cts - R(4) * css * Prim[D::nbmd] * Prim[D::nbmd] * rhoinv)) / R(2));
   Cons[mvel] = Prim[D::nved];
   Cons[mpre] = ptl;
 }
@@ -592,7 +609,7 @@ __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPR
   const R emag = R(0.5) * (u[mbm1] * u[mbm1] + u[mbm2] * u[mbm2] + u[mbm3] * u[mbm3]);
   p[nene] = kFast ? (u[meto] - ekin - emag) * rhoinv : (u[meto] - ekin - emag) / u[mden];
   p[npre] = p[nene] * p[nden] * (gam - R(1));
-  p[ncsp] = fsqrt(p[nene] * gam * (gam - R(1)));
+  p[ncsp] = fsqrt_est(p[nene] * gam * (gam - R(1)));  // the sound speed only enters wave-speed estimates
   p[nbm1] = u[mbm1];
   p[nbm2] = u[mbm2];
   p[nbm3] = u[mbm3];
@@ -603,7 +620,7 @@ __device__ __forceinline__ void cons2prim(const R (&u)[NCONS], R gam, R (&p)[NPR
 // Per-cell CFL time (ControlTimestep, mhd.cpp:1542-1550): min over d of dx_d/(|v_d| + ctot).
 template <class R>
 __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
-  const R ctot = fsqrt(p[ncsp] * p[ncsp] + fdiv_est(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
+  const R ctot = fsqrt_est(p[ncsp] * p[ncsp] + fdiv_est(p[nbm1] * p[nbm1] + p[nbm2] * p[nbm2] + p[nbm3] * p[nbm3], p[nden]));
   R dt = fdiv_est(dx, fabs(p[nve1]) + ctot);
   const R b = fdiv_est(dy, fabs(p[nve2]) + ctot);
   const R c = fdiv_est(dz, fabs(p[nve3]) + ctot);
@@ -621,11 +638,11 @@ __device__ __forceinline__ R cell_ch(const R (&p)[NPRIM]) {
   const R ca2 = kFast ? p[nbm2] * p[nbm2] * ri : p[nbm2] * p[nbm2] / p[nden];
   const R ca3 = kFast ? p[nbm3] * p[nbm3] * ri : p[nbm3] * p[nbm3] / p[nden];
   const R cts = css + ca1 + ca2 + ca3;
-  const R cm1 = fsqrt((cts + fsqrt(cts * cts - R(4) * css * ca1)) / R(2));
+  const R cm1 = fsqrt_est((cts + fsqrt_est(cts * cts - R(4) * css * ca1)) / R(2));
   const R ch1 = (fabs(p[nve1]) + cm1);
-  const R cm2 = fsqrt((cts + fsqrt(cts * cts - R(4) * css * ca2)) / R(2));
+  const R cm2 = fsqrt_est((cts + fsqrt_est(cts * cts - R(4) * css * ca2)) / R(2));
   const R ch2 = (fabs(p[nve2]) + cm2);
-  const R cm3 = fsqrt((cts + fsqrt(cts * cts - R(4) * css * ca3)) / R(2));
+  const R cm3 = fsqrt_est((cts + fsqrt_est(cts * cts - R(4) * css * ca3)) / R(2));
   const R ch3 = (fabs(p[nve3]) + cm3);
   R m = ch1;
   if (m < ch2) m = ch2;
