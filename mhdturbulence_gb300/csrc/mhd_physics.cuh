@@ -31,6 +31,11 @@ namespace MHDGB_VNS {
 // reference's expressions and IEEE division.
 constexpr bool kFast = MHDGB_FAST != 0;
 
+// x with its sign flipped when neg (a bit operation on the integer pipe, not an FP64 instruction).
+__device__ __forceinline__ double negate_if(double x, bool neg) {
+  return __hiloint2double(__double2hiint(x) ^ (neg ? (int)0x80000000 : 0), __double2loint(x));
+}
+
 // FP64 reciprocal from an FP32 seed (integer-pipe narrowing, the MUFU approximate reciprocal) and two
 // Newton-Raphson steps r <- r + r(1 - b r): the error of the seed (~2^-22) squares at each step,
 // so the result is within about one ulp of 1/b.
@@ -387,21 +392,28 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   const R bxs = R(0.5) * (leftst[mubu] + rigtst[mubu]);
   const R bxsq = bxs * bxs;
   const bool left = !signbit(sm);  // copysign(1, sm) > 0, mhd.cpp:384
+  // The left side's clamps min(-1e-20, x) and min(x, 0) are the right side's max(1e-20, -x) and
+  // max(-x, 0) negated: each selection is one max on the chosen side with sign flips (bit
+  // operations) instead of both arms.
+  auto side_max = [&](R floor_, R x, bool neg) { return negate_if(smax(floor_, negate_if(x, neg)), neg); };
   // upwind side only: s = side speed, sd = s - v, sdm = s - sm, ro/e/v/b of that side
   const R s_ = left ? sl : sr;
   const R sd = left ? sdl : sdr;
   const R rosd = left ? rosdl : rosdr;
-  const R sdm = left ? smin(R(-1e-20), sl - sm) : smax(R(1e-20), sr - sm);
+  const R sdm = side_max(R(1e-20), s_ - sm, left);
   const R ro = left ? rol : ror, ee = left ? eel : eer, pt = left ? ptl : ptr;
   const R vx = left ? vxl : vxr, vy = left ? vyl : vyr, vz = left ? vzl : vzr;
   const R by = left ? byl : byr, bz = left ? bzl : bzr;
   const R sc = left ? Pl[nst] : Pr[nst];
-  // star state of the upwind side (Step 5A/5B)
-  R rost = ro, vxst = vx, vyst = vy, vzst = vz, byst = by, bzst = bz, eest = ee;
+  // star state of the upwind side (Step 5A/5B); one reciprocal of sdm * T gives 1/sdm and 1/T
+  R rost = ro, vxst = vx, vyst = vy, vzst = vz, byst = by, bzst = bz;
   const R temp_fst = rosd * sdm - bxsq;
-  const R isdm = fdiv(R(1), sdm);
-  if (!(fabs(temp_fst) - eps < R(0))) {
-    const R itf = fdiv(R(1), temp_fst);
+  const bool nondeg = !(fabs(temp_fst) - eps < R(0));
+  R isdm = R(0);
+  if (nondeg) {
+    const R rr = fdiv(R(1), sdm * temp_fst);
+    isdm = temp_fst * rr;
+    const R itf = sdm * rr;
     const R t1 = bxs * (sd - sdm) * itf;
     rost = rosd * isdm;
     vxst = sm;
@@ -410,22 +422,23 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
     const R t2 = (rosd * sd - bxsq) * itf;
     byst = by * t2;
     bzst = bz * t2;
-    const R vdbst = vxst * bxs + vyst * byst + vzst * bzst;
-    eest = (sd * ee - pt * vx + ptst * sm + bxs * (vx * bxs + vy * by + vz * bz - vdbst)) * isdm;
   }
+  const R vdbst = vxst * bxs + vyst * byst + vzst * bzst;
+  const R eest = nondeg ? (sd * ee - pt * vx + ptst * sm + bxs * (vx * bxs + vy * by + vz * bz - vdbst)) * isdm : ee;
   // Alfven (double-star) correction of the tangential states and energy (Step 5C), needs both
   // star states: the other side's star state is formed the same way.
   const R so_sd = left ? sdr : sdl;
   const R so_rosd = left ? rosdr : rosdl;
-  const R so_sdm = left ? smax(R(1e-20), sr - sm) : smin(R(-1e-20), sl - sm);
+  const R so_sdm = side_max(R(1e-20), (left ? sr : sl) - sm, !left);
   const R so_ro = left ? ror : rol;
   const R so_vy = left ? vyr : vyl, so_vz = left ? vzr : vzl, so_by = left ? byr : byl, so_bz = left ? bzr : bzl;
   R so_rost = so_ro, so_vyst = so_vy, so_vzst = so_vz, so_byst = so_by, so_bzst = so_bz;
   const R so_tf = so_rosd * so_sdm - bxsq;
   if (!(fabs(so_tf) - eps < R(0))) {
-    const R itf = fdiv(R(1), so_tf);
+    const R rr = fdiv(R(1), so_sdm * so_tf);
+    const R itf = so_sdm * rr;
     const R t1 = bxs * (so_sd - so_sdm) * itf;
-    so_rost = so_rosd * fdiv(R(1), so_sdm);
+    so_rost = so_rosd * (so_tf * rr);
     so_vyst = so_vy - so_by * t1;
     so_vzst = so_vz - so_bz * t1;
     const R t2 = (so_rosd * so_sd - bxsq) * itf;
@@ -433,9 +446,9 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
     so_bzst = so_bz * t2;
   }
   const R abbx = fabs(bxs);
+  const bool bneg = signbit(bxs);  // signbx = copysign(1, bxs) < 0
   R vydst = vyst, vzdst = vzst, bydst = byst, bzdst = bzst, eedst = eest, sst = R(0);
   if (!(abbx - eps < R(0))) {
-    const R signbx = copysign(R(1), bxs);
     // sqrt of the upwind star density and its reciprocal from one Goldschmidt iteration
     R sq, isq;
     if (sqrt_seed_range(rost)) {
@@ -452,18 +465,20 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
     const R vzl_st = left ? vzst : so_vzst, vzr_st = left ? so_vzst : vzst;
     const R byl_st = left ? byst : so_byst, byr_st = left ? so_byst : byst;
     const R bzl_st = left ? bzst : so_bzst, bzr_st = left ? so_bzst : bzst;
-    vydst = invsumro * (sql * vyl_st + sqr * vyr_st + signbx * (byr_st - byl_st));
-    vzdst = invsumro * (sql * vzl_st + sqr * vzr_st + signbx * (bzr_st - bzl_st));
-    bydst = invsumro * (sql * byr_st + sqr * byl_st + signbx * sql * sqr * (vyr_st - vyl_st));
-    bzdst = invsumro * (sql * bzr_st + sqr * bzl_st + signbx * sql * sqr * (vzr_st - vzl_st));
-    const R vdbst = vxst * bxs + vyst * byst + vzst * bzst;
+    vydst = invsumro * (sql * vyl_st + sqr * vyr_st + negate_if(byr_st - byl_st, bneg));
+    vzdst = invsumro * (sql * vzl_st + sqr * vzr_st + negate_if(bzr_st - bzl_st, bneg));
+    const R sgq = negate_if(sql * sqr, bneg);  // signbx * sqrtrol * sqrtror
+    bydst = invsumro * (sql * byr_st + sqr * byl_st + sgq * (vyr_st - vyl_st));
+    bzdst = invsumro * (sql * bzr_st + sqr * bzl_st + sgq * (vzr_st - vzl_st));
     const R tdd = sm * bxs + vydst * bydst + vzdst * bzdst;
-    eedst = left ? eest - sq * signbx * (vdbst - tdd) : eest + sq * signbx * (vdbst - tdd);
-    sst = left ? sm - abbx * isq : sm + abbx * isq;
+    // left: eest - sq signbx (vdbst - tdd); right: eest + sq signbx (vdbst - tdd)
+    eedst = eest + negate_if(sq * (vdbst - tdd), bneg != left);
+    // left: sm - |bx|/sq; right: sm + |bx|/sq
+    sst = sm + negate_if(abbx * isq, left);
   }
-  // Step 6: flux of the upwind side
-  const R ms = left ? smin(s_, R(0)) : smax(s_, R(0));
-  const R msst = left ? smin(sst, R(0)) : smax(sst, R(0));
+  // Step 6: flux of the upwind side (ms = min(s, 0) on the left, max(s, 0) on the right)
+  const R ms = side_max(R(0), s_, left);
+  const R msst = side_max(R(0), sst, left);
   const R* cst = left ? leftst : rigtst;
   const R rx = cst[muvu], ry = cst[muvv], rz = cst[muvw];
   nflux[mden] = cst[mfdn] + (rost - ro) * ms;
