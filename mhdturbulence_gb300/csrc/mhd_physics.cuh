@@ -31,6 +31,24 @@ namespace MHDGB_VNS {
 // reference's expressions and IEEE division.
 constexpr bool kFast = MHDGB_FAST != 0;
 
+// Comparisons of doubles on the integer pipe.  GB300 issues FP64 compares and min/max on the FP64
+// pipe, which bounds the FP64 form; the integer pipe is nearly idle.  For non-NaN arguments these
+// give the results of the FP64 comparisons (min/max order -0 below +0, which only changes the sign of
+// a zero).
+__device__ __forceinline__ bool pos_nonzero(double x) {  // x > 0
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b <= 0x7FF0000000000000LL;
+}
+__device__ __forceinline__ bool abs_less(double x, double lim) {  // |x| < lim, for a finite lim > 0
+  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) < __double_as_longlong(lim);
+}
+__device__ __forceinline__ long long order_key(double x) {  // monotone in x
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ double imin(double a, double b) { return order_key(b) < order_key(a) ? b : a; }
+__device__ __forceinline__ double imax(double a, double b) { return order_key(a) < order_key(b) ? b : a; }
+
 // x with its sign flipped when neg (a bit operation on the integer pipe, not an FP64 instruction).
 __device__ __forceinline__ double negate_if(double x, bool neg) {
   return __hiloint2double(__double2hiint(x) ^ (neg ? (int)0x80000000 : 0), __double2loint(x));
@@ -141,7 +159,10 @@ template <class R>
 __device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
   if constexpr (kFast) {  // one product for the test and the numerator: p + p == (2 dsvp) dsvm exactly
     const R p = dsvp * dsvm;
-    return (p > R(0)) ? fdiv_est(p + p, dsvp + dsvm) : R(0);
+    bool pos;
+    if constexpr (std::is_same<R, double>::value) pos = pos_nonzero(p);
+    else pos = p > R(0);
+    return pos ? fdiv_est(p + p, dsvp + dsvm) : R(0);
   } else {
     return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
   }
@@ -379,11 +400,12 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   const R vxr = Pr[D::nved], vyr = Pr[D::nvef], vzr = Pr[D::nveb];
   const R byr = rigtst[mubv], bzr = rigtst[mubw], ptr = rigtst[mpre];
   const R cfl = leftst[mcsp], cfr = rigtst[mcsp];
-  const R cmax = smax(cfl, cfr);
-  const R sl = smin(vxl, vxr) - cmax;
-  const R sr = smax(vxl, vxr) + cmax;
-  const R sdl = smin(R(-1e-20), sl - vxl);
-  const R sdr = smax(R(1e-20), sr - vxr);
+  // min/max and the eps tests below are integer-pipe comparisons (imin, imax, abs_less)
+  const R cmax = imax(cfl, cfr);
+  const R sl = imin(vxl, vxr) - cmax;
+  const R sr = imax(vxl, vxr) + cmax;
+  const R sdl = imin(R(-1e-20), sl - vxl);
+  const R sdr = imax(R(1e-20), sr - vxr);
   const R rosdl = rol * sdl;
   const R rosdr = ror * sdr;
   const R tden = fdiv(R(1), rosdr - rosdl);
@@ -395,7 +417,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   // The left side's clamps min(-1e-20, x) and min(x, 0) are the right side's max(1e-20, -x) and
   // max(-x, 0) negated: each selection is one max on the chosen side with sign flips (bit
   // operations) instead of both arms.
-  auto side_max = [&](R floor_, R x, bool neg) { return negate_if(smax(floor_, negate_if(x, neg)), neg); };
+  auto side_max = [&](R floor_, R x, bool neg) { return negate_if(imax(floor_, negate_if(x, neg)), neg); };
   // upwind side only: s = side speed, sd = s - v, sdm = s - sm, ro/e/v/b of that side
   const R s_ = left ? sl : sr;
   const R sd = left ? sdl : sdr;
@@ -408,7 +430,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   // star state of the upwind side (Step 5A/5B); one reciprocal of sdm * T gives 1/sdm and 1/T
   R rost = ro, vxst = vx, vyst = vy, vzst = vz, byst = by, bzst = bz;
   const R temp_fst = rosd * sdm - bxsq;
-  const bool nondeg = !(fabs(temp_fst) - eps < R(0));
+  const bool nondeg = !abs_less(temp_fst, eps);
   R isdm = R(0);
   if (nondeg) {
     const R rr = fdiv(R(1), sdm * temp_fst);
@@ -434,7 +456,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   const R so_vy = left ? vyr : vyl, so_vz = left ? vzr : vzl, so_by = left ? byr : byl, so_bz = left ? bzr : bzl;
   R so_rost = so_ro, so_vyst = so_vy, so_vzst = so_vz, so_byst = so_by, so_bzst = so_bz;
   const R so_tf = so_rosd * so_sdm - bxsq;
-  if (!(fabs(so_tf) - eps < R(0))) {
+  if (!abs_less(so_tf, eps)) {
     const R rr = fdiv(R(1), so_sdm * so_tf);
     const R itf = so_sdm * rr;
     const R t1 = bxs * (so_sd - so_sdm) * itf;
@@ -448,7 +470,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   const R abbx = fabs(bxs);
   const bool bneg = signbit(bxs);  // signbx = copysign(1, bxs) < 0
   R vydst = vyst, vzdst = vzst, bydst = byst, bzdst = bzst, eedst = eest, sst = R(0);
-  if (!(abbx - eps < R(0))) {
+  if (!abs_less(bxs, eps)) {
     // sqrt of the upwind star density and its reciprocal from one Goldschmidt iteration
     R sq, isq;
     if (sqrt_seed_range(rost)) {
