@@ -169,8 +169,15 @@ __device__ __forceinline__ void recover_cell<double>(const double (&u)[NCONS], d
   write_ghost_images<double>(Pout, L, bc, ii, jj, kk, p);
   dtc = cell_dt<double>(p, dx, dy, dz);
   chc = cell_ch<double>(p);
-  if (!(dtc == dtc) || !(chc == chc) || isinf(chc)) bad |= ST_NONFINITE;
-  if (!(p[nden] > 0.0) || !(p[npre] > 0.0)) bad |= ST_NEGATIVE;
+  if constexpr (kFast) {  // the same tests on the integer pipe (dtc NaN; chc NaN or inf; rho, p > 0)
+    const long long abs_mask = 0x7FFFFFFFFFFFFFFFLL, inf_bits = 0x7FF0000000000000LL;
+    if ((__double_as_longlong(dtc) & abs_mask) > inf_bits || (__double_as_longlong(chc) & inf_bits) == inf_bits)
+      bad |= ST_NONFINITE;
+    if (!pos_nonzero(p[nden]) || !pos_nonzero(p[npre])) bad |= ST_NEGATIVE;
+  } else {
+    if (!(dtc == dtc) || !(chc == chc) || isinf(chc)) bad |= ST_NONFINITE;
+    if (!(p[nden] > 0.0) || !(p[npre] > 0.0)) bad |= ST_NEGATIVE;
+  }
 }
 
 // Mixed form: the specific internal energy e = (E - m^2/(2 rho) - B^2/2)/rho is computed in FP64
@@ -520,8 +527,13 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         R dtc, chc;
         recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, k, spacing_of<R>(a, 0, ii + NGH),
                         spacing_of<R>(a, 1, jj + NGH), spacing_of<R>(a, 2, k + NGH), dtc, chc, bad);
-        cmin = smin(cmin, dtc);
-        cmax = smax(cmax, chc);
+        if constexpr (kFast && std::is_same<R, double>::value) {  // integer-pipe min/max
+          cmin = imin(cmin, dtc);
+          cmax = imax(cmax, chc);
+        } else {
+          cmin = smin(cmin, dtc);
+          cmax = smax(cmax, chc);
+        }
       }
       zb ^= 1;
     }

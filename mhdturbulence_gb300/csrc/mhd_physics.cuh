@@ -661,6 +661,7 @@ __device__ __forceinline__ R cell_dt(const R (&p)[NPRIM], R dx, R dy, R dz) {
   R dt = fdiv_est(dx, fabs(p[nve1]) + ctot);
   const R b = fdiv_est(dy, fabs(p[nve2]) + ctot);
   const R c = fdiv_est(dz, fabs(p[nve3]) + ctot);
+  if constexpr (kFast && std::is_same<R, double>::value) return imin(imin(dt, b), c);  // integer pipe
   if (b < dt) dt = b;
   if (c < dt) dt = c;
   return dt;
@@ -682,6 +683,7 @@ __device__ __forceinline__ R cell_ch(const R (&p)[NPRIM]) {
   const R cm3 = fsqrt_est((cts + fsqrt_est(cts * cts - R(4) * css * ca3)) / R(2));
   const R ch3 = (fabs(p[nve3]) + cm3);
   R m = ch1;
+  if constexpr (kFast && std::is_same<R, double>::value) return imax(imax(m, ch2), ch3);  // integer pipe
   if (m < ch2) m = ch2;
   if (m < ch3) m = ch3;
   return m;
