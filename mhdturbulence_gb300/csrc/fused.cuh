@@ -234,10 +234,16 @@ __device__ __forceinline__ void update_cell(const DivAcc<double>& acc, const dou
                                             int k, double (&u)[NCONS]) {
 #pragma unroll
   for (int m = 0; m < NCONS; m++) u[m] = Uc[m * fs] - dt * acc.s[m];
-  double dhl = a.dxs[i];
-  if (a.dys[j] < dhl) dhl = a.dys[j];
-  if (a.dzs[k] < dhl) dhl = a.dzs[k];
-  const double taui = 0.1 * chd / dhl;
+  double taui;
+  if constexpr (kFast) {  // integer-pipe min of the (positive) spacings, Newton-reciprocal division
+    const double dhl = imin(imin(a.dxs[i], a.dys[j]), a.dzs[k]);
+    taui = fdiv(0.1 * chd, dhl);
+  } else {
+    double dhl = a.dxs[i];
+    if (a.dys[j] < dhl) dhl = a.dys[j];
+    if (a.dzs[k] < dhl) dhl = a.dzs[k];
+    taui = 0.1 * chd / dhl;
+  }
   u[mbps] = u[mbps] * (1.0 - dt * taui);
 }
 
