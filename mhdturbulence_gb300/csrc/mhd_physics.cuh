@@ -232,6 +232,52 @@ __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC
   Cons[mpre] = ptl;
 }
 
+// Prim2ConsD split in two for the FP64 branch-form HLLD, which needs the physical flux of the
+// upwind side only: the state part (conserved variables, fast speed, normal velocity, total
+// pressure) for both sides, then the flux part for the chosen side, with prim2cons's expressions.
+template <class R, int DIR>
+__device__ __forceinline__ void prim2cons_state(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
+  using D = Dir<DIR>;
+  const R rho = Prim[nden];
+  const R rhoinv = fdiv_est(R(1), rho);
+  const R vsq = Prim[nve1] * Prim[nve1] + Prim[nve2] * Prim[nve2] + Prim[nve3] * Prim[nve3];
+  const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
+  Cons[mudn] = rho;
+  Cons[D::muv1] = rho * Prim[nve1];
+  Cons[D::muv2] = rho * Prim[nve2];
+  Cons[D::muv3] = rho * Prim[nve3];
+  Cons[muet] = rho * Prim[nene] + R(0.5) * rho * vsq + R(0.5) * bsq;
+  Cons[D::mub1] = Prim[nbm1];
+  Cons[D::mub2] = Prim[nbm2];
+  Cons[D::mub3] = Prim[nbm3];
+  Cons[mubp] = Prim[nbps];
+  Cons[must] = rho * Prim[nst];
+  const R css = Prim[ncsp] * Prim[ncsp];
+  const R cts = css + bsq * rhoinv;
+  Cons[mcsp] = fsqrt_est((cts + fsqrt_est(cts * cts - R(4) * css * Prim[D::nbmd] * Prim[D::nbmd] * rhoinv)) / R(2));
+  Cons[mvel] = Prim[D::nved];
+  Cons[mpre] = Prim[npre] + bsq / R(2);
+}
+// The flux slots (mfdn .. mfst) of Cons from the primitive state and Cons[muet], Cons[mpre].
+template <class R, int DIR>
+__device__ __forceinline__ void prim2cons_flux(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
+  using D = Dir<DIR>;
+  const R rho = Prim[nden];
+  const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
+  const R ptl = Cons[mpre];
+  Cons[mfdn] = rho * Prim[D::nved];
+  Cons[D::mfv1] = rho * Prim[nve1] * Prim[D::nved] - Prim[nbm1] * Prim[D::nbmd];
+  Cons[D::mfv2] = rho * Prim[nve2] * Prim[D::nved] - Prim[nbm2] * Prim[D::nbmd];
+  Cons[D::mfv3] = rho * Prim[nve3] * Prim[D::nved] - Prim[nbm3] * Prim[D::nbmd];
+  Cons[mfet] = (Cons[muet] + ptl) * Prim[D::nved] - bsq * Prim[D::nbmd];
+  Cons[mfvu] += ptl;
+  Cons[mfbu] = R(0);
+  Cons[mfbv] = Prim[D::nbmf] * Prim[D::nved] - Prim[D::nvef] * Prim[D::nbmd];
+  Cons[mfbw] = Prim[D::nbmb] * Prim[D::nved] - Prim[D::nveb] * Prim[D::nbmd];
+  Cons[mfbp] = R(0);
+  Cons[mfst] = rho * Prim[nst] * Prim[D::nved];
+}
+
 // HLLD, mhd.cpp:97-417.  Writes the 10 rotated fluxes (slot mubp is left undefined: the GLM pair
 // replaces it).
 // Fast forms: the velocities m/rho of the rotated states are the reconstructed primitive
@@ -501,7 +547,14 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   // Step 6: flux of the upwind side (ms = min(s, 0) on the left, max(s, 0) on the right)
   const R ms = side_max(R(0), s_, left);
   const R msst = side_max(R(0), sst, left);
-  const R* cst = left ? leftst : rigtst;
+  // physical flux of the upwind side only (its state part is already in leftst / rigtst)
+  R cst[NVEC];
+#pragma unroll
+  for (int q = 0; q < NVEC; q++) cst[q] = left ? leftst[q] : rigtst[q];
+  R pup[NPRIM];
+#pragma unroll
+  for (int n = 0; n < NPRIM; n++) pup[n] = left ? Pl[n] : Pr[n];
+  prim2cons_flux<R, DIR>(pup, cst);
   const R rx = cst[muvu], ry = cst[muvv], rz = cst[muvw];
   nflux[mden] = cst[mfdn] + (rost - ro) * ms;
   nflux[meto] = cst[mfet] + (eest - ee) * ms + (eedst - eest) * msst;
@@ -605,14 +658,20 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
                                           int riemann = RIEMANN_HLLD) {
   using D = Dir<DIR>;
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
-  prim2cons<R, DIR>(Pl, Cl);
-  prim2cons<R, DIR>(Pr, Cr);
+  constexpr bool branch_hlld = kFast && std::is_same<R, double>::value;
+  if (branch_hlld && riemann == RIEMANN_HLLD) {  // the upwind flux is formed inside hlld_branch
+    prim2cons_state<R, DIR>(Pl, Cl);
+    prim2cons_state<R, DIR>(Pr, Cr);
+  } else {
+    prim2cons<R, DIR>(Pl, Cl);
+    prim2cons<R, DIR>(Pr, Cr);
+  }
   if (riemann == RIEMANN_HLLE) {
     hlle<R, DIR>(Cl, Cr, nf);
   } else if (riemann == RIEMANN_HLLC) {
     hllc<R, DIR>(Cl, Cr, Pl, Pr, nf);
   } else {
-    if constexpr (kFast && std::is_same<R, double>::value) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf);
+    if constexpr (branch_hlld) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf);
     else hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
   }
   F[mden] = nf[mden];
