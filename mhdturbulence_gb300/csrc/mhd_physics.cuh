@@ -54,6 +54,14 @@ __device__ __forceinline__ double negate_if(double x, bool neg) {
   return __hiloint2double(__double2hiint(x) ^ (neg ? (int)0x80000000 : 0), __double2loint(x));
 }
 
+// FP32 counterparts for the mixed form's solver (FP32 compares are cheap; these keep one code path).
+__device__ __forceinline__ float negate_if(float x, bool neg) {
+  return __int_as_float(__float_as_int(x) ^ (neg ? (int)0x80000000 : 0));
+}
+__device__ __forceinline__ bool abs_less(float x, float lim) { return fabsf(x) < lim; }
+__device__ __forceinline__ float imin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float imax(float a, float b) { return (a < b) ? b : a; }
+
 // FP64 reciprocal from an FP32 seed (integer-pipe narrowing, the MUFU approximate reciprocal) and two
 // Newton-Raphson steps r <- r + r(1 - b r): the error of the seed (~2^-22) squares at each step,
 // so the result is within about one ulp of 1/b.
@@ -427,13 +435,12 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   nflux[mbps] = R(0);
 }
 
-// HLLD in branch form, for the FMA-contracted FP64 build.  Same states and fluxes as hlld(), but the selections
-// the reference performs with 0/1 masks (maxs1/mins1 of mhd.cpp:272-275, 306-308, 343-346, 384-386)
-// are branches: the degenerate-field forms are taken only when their conditions hold, and only the
-// upwind side of the final flux is formed.  Results agree with hlld() to rounding (and in the sign
-// of zero results).  On GB300 it cuts the FP64 step by about 16%; the FP32 reconstruction of the
-// mixed form is issue-latency bound rather than FP64-pipe bound and keeps the mask form, which
-// measured slightly faster there.
+// HLLD in branch form, for the FMA-contracted builds (FP64 and the mixed form's FP32 solve).  Same
+// states and fluxes as hlld(), but the selections the reference performs with 0/1 masks
+// (maxs1/mins1 of mhd.cpp:272-275, 306-308, 343-346, 384-386) are branches: the degenerate-field
+// forms are taken only when their conditions hold, and only the upwind side's physical flux is
+// formed (face_flux() passes states without flux slots; prim2cons_flux() fills the upwind side's).
+// Results agree with hlld() to rounding (and in the sign of zero results).
 template <class R, int DIR>
 __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], const R (&Pl)[NPRIM],
                                             const R (&Pr)[NPRIM], R (&nflux)[NCONS]) {
@@ -476,7 +483,9 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   // star state of the upwind side (Step 5A/5B); one reciprocal of sdm * T gives 1/sdm and 1/T
   R rost = ro, vxst = vx, vyst = vy, vzst = vz, byst = by, bzst = bz;
   const R temp_fst = rosd * sdm - bxsq;
-  const bool nondeg = !abs_less(temp_fst, eps);
+  // FP32: the degenerate-state guard relative to the star total pressure (see hlld())
+  const R deg = std::is_same<R, float>::value ? imax(eps, R(3e-4) * fabs(ptst)) : eps;
+  const bool nondeg = !abs_less(temp_fst, deg);
   R isdm = R(0);
   if (nondeg) {
     const R rr = fdiv(R(1), sdm * temp_fst);
@@ -502,7 +511,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   const R so_vy = left ? vyr : vyl, so_vz = left ? vzr : vzl, so_by = left ? byr : byl, so_bz = left ? bzr : bzl;
   R so_rost = so_ro, so_vyst = so_vy, so_vzst = so_vz, so_byst = so_by, so_bzst = so_bz;
   const R so_tf = so_rosd * so_sdm - bxsq;
-  if (!abs_less(so_tf, eps)) {
+  if (!abs_less(so_tf, deg)) {
     const R rr = fdiv(R(1), so_sdm * so_tf);
     const R itf = so_sdm * rr;
     const R t1 = bxs * (so_sd - so_sdm) * itf;
@@ -519,8 +528,13 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   if (!abs_less(bxs, eps)) {
     // sqrt of the upwind star density and its reciprocal from one Goldschmidt iteration
     R sq, isq;
-    if (sqrt_seed_range(rost)) {
-      sq = sqrt_goldschmidt(rost, &isq);
+    if constexpr (std::is_same<R, double>::value) {
+      if (sqrt_seed_range(rost)) {
+        sq = sqrt_goldschmidt(rost, &isq);
+      } else {
+        sq = sqrt(rost);
+        isq = R(1) / sq;
+      }
     } else {
       sq = sqrt(rost);
       isq = R(1) / sq;
@@ -658,7 +672,7 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
                                           int riemann = RIEMANN_HLLD) {
   using D = Dir<DIR>;
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
-  constexpr bool branch_hlld = kFast && std::is_same<R, double>::value;
+  constexpr bool branch_hlld = kFast;
   if (branch_hlld && riemann == RIEMANN_HLLD) {  // the upwind flux is formed inside hlld_branch
     prim2cons_state<R, DIR>(Pl, Cl);
     prim2cons_state<R, DIR>(Pr, Cr);

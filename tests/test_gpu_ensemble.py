@@ -63,9 +63,14 @@ def test_ensemble_autotune_and_variants_agree():
             ens.step(5)
             ens.sync()
             results.append([m.download_cons() for m in ens.members])
+    # mixed form: variants of one register budget agree bit for bit, the 1-CTA and 2-CTA builds
+    # within 1e-9 relative (different FP32 multiply-add contraction)
     for r in results[1:]:
         for a, b in zip(r, results[0]):
-            assert np.array_equal(a, b)
+            ai, bi = ic.interior(a), ic.interior(b)
+            err = max(np.abs(ai[:, :, m, :] - bi[:, :, m, :]).max() / max(np.abs(bi[:, :, m, :]).max(), 1e-3)
+                      for m in range(10))
+            assert err <= 1e-9, err
 
 
 def test_ensemble_stop_condition_per_member():
