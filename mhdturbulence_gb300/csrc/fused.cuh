@@ -326,6 +326,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     const double dt = a.cfl * bitsd(cur_slot.dtmin_bits);
     const double chd = bitsd(cur_slot.chmax_bits);
     const R chg = (R)chd;
+    const GlmConst<R> glm = glm_const(chg);
     const int riemann = GEN ? a.riemann : (int)RIEMANN_HLLD;
     const float dtf = (float)dt, chf = (float)chd;
     RedSlot* next = &ctrl->slot[(step + 1) % 3];
@@ -451,7 +452,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
               pl[n] = left_state(PV(pk, n, i - 1, j), SLX(n, i - 1, j));
               pr[n] = right_state(PV(pk, n, i, j), SLX(n, i, j));
             }
-            face_flux<R, 1>(pl, pr, chg, f, riemann);
+            face_flux<R, 1>(pl, pr, glm, f, riemann);
 #pragma unroll
             for (int m = 0; m < NCONS; m++) FXS(m, i, j) = f[m];
           }
@@ -464,7 +465,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
               pl[n] = left_state(PV(pk, n, i, j - 1), SLY(n, i, j - 1));
               pr[n] = right_state(PV(pk, n, i, j), SLY(n, i, j));
             }
-            face_flux<R, 2>(pl, pr, chg, f, riemann);
+            face_flux<R, 2>(pl, pr, glm, f, riemann);
 #pragma unroll
             for (int m = 0; m < NCONS; m++) FYS(m, i, j) = f[m];
           }
@@ -482,7 +483,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
               pl[n] = left_state(PV(pa, n, i, j), SLZ(sa, n, i, j));
               pr[n] = right_state(PV(pb, n, i, j), SLZ(sb, n, i, j));
             }
-            face_flux<R, 3>(pl, pr, chg, f, riemann);
+            face_flux<R, 3>(pl, pr, glm, f, riemann);
             // the lower face overwrites the slopes it alone read (column (i, j) of buffer 2)
 #pragma unroll
             for (int m = 0; m < NCONS; m++) {

@@ -44,7 +44,7 @@ __global__ void k_flux(const double* __restrict__ P, double* __restrict__ F, Lay
     Pr[n] = right_state(R1[n], van_leer(R2[n] - R1[n], R1[n] - L2[n]));
   }
   double f[NCONS];
-  face_flux<double, DIR>(Pl, Pr, chg, f, riemann);
+  face_flux<double, DIR>(Pl, Pr, glm_const(chg), f, riemann);
 #pragma unroll
   for (int m = 0; m < NCONS; m++) F[L.at(NCONS, m, k, j, i)] = f[m];
 }
