@@ -159,6 +159,18 @@ __device__ __forceinline__ R fdiv_est(R a, R b) {
   }
 }
 
+// 2p / s at the accuracy of fdiv_est, with the factor 2 taken into the FP32 seed (exact there):
+// y0 = 2 r0 and one Newton step y1 = y0 + r0 (2 - s y0) = 2 r0 (2 - s r0).  One FP64 operation fewer
+// than fdiv_est(p + p, s).
+__device__ __forceinline__ double twice_div_est(double p, double s) {
+  const unsigned e = ((unsigned)__double2hiint(s) >> 20) & 0x7FFu;
+  if (e < 1023u - 120u || e > 1023u + 120u) return (p + p) / s;
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d2f_rne(s)));
+  const double h = f2d_exact(r0), y0 = f2d_exact(2.0f * r0);
+  return p * fma(h, fma(-s, y0, 2.0), y0);
+}
+
 // vanLeer, src_cpp_kokkos_host/mhd.cpp:89-95.  The limited slope of a cell c is
 // van_leer(P[c+1]-P[c], P[c]-P[c-1]); the reference evaluates the same expression for the left
 // state of face c+1/2 and the right state of face c-1/2 (mhd.cpp:1134-1154), so one evaluation
@@ -167,10 +179,11 @@ template <class R>
 __device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
   if constexpr (kFast) {  // one product for the test and the numerator: p + p == (2 dsvp) dsvm exactly
     const R p = dsvp * dsvm;
-    bool pos;
-    if constexpr (std::is_same<R, double>::value) pos = pos_nonzero(p);
-    else pos = p > R(0);
-    return pos ? fdiv_est(p + p, dsvp + dsvm) : R(0);
+    if constexpr (std::is_same<R, double>::value) {
+      return pos_nonzero(p) ? twice_div_est(p, dsvp + dsvm) : R(0);
+    } else {
+      return (p > R(0)) ? fdiv_est(p + p, dsvp + dsvm) : R(0);
+    }
   } else {
     return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
   }
