@@ -279,6 +279,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::bar_off);
   int& s_item = *reinterpret_cast<int*>(smem + S::misc_off);
   int& s_abort = *reinterpret_cast<int*>(smem + S::misc_off + 4);
+  int& s_aitem = *reinterpret_cast<int*>(smem + S::misc_off + 8);  // next phase-A warp item
 
   const int tid = threadIdx.x;
   const int ninst = (int)lc->ninst, total = (int)lc->total_items;
@@ -295,6 +296,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     for (int s = 0; s < NBUF; s++) mbar_init(&bars[s], 1);
     fence_mbar_init();
     s_abort = 0;
+    s_aitem = 0;
   }
   __syncthreads();
 
@@ -402,11 +404,19 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     // Two barriers per plane.  Phase A writes only slope buffers that the previous plane's phase C
     // does not read, and phase C reads no ring plane, so neither the start nor the end of a plane
     // needs a barrier; the ring slot of plane k is reloaded once phase B has read it.
+    // Phase A hands out whole-warp items from a shared counter: the warps without a cell (no phase
+    // C) start on the slopes at once and the owner warps join when their cells are done.
+    const int nwa = (pxs + pys + pzs) >> 5;
     for (int k = kb; k < ke; k++) {
       wait_plane(k + 2);
       const R *pk = plane(k), *pk1 = plane(k + 1), *pk2 = plane(k + 2);
       // ---- phase A: slopes ----
-      for (int q = tid; q < pxs + pys + pzs; q += NT) {
+      for (;;) {
+        int w = 0;
+        if ((tid & 31) == 0) w = atomicAdd(&s_aitem, 1);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= nwa) break;
+        const int q = (w << 5) | (tid & 31);
         if (q < pxs) {
           if (q < nxs) {
             const int j = q / (cx + 2), i = q % (cx + 2) - 1;
@@ -441,6 +451,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       __syncthreads();
       if (s_abort) break;  // a plane that never arrived (bounded wait): the data above is not used
       // ---- phase B: face fluxes (on the first plane also the faces kb-1/2, into slope buffer 2) ----
+      if (tid == 0) s_aitem = 0;  // every warp has left phase A; the barrier after phase B publishes it
       const int nq = pxf + pyf + (k == kb ? 2 * pzf : pzf);
       for (int q = tid; q < nq; q += NT) {
         R pl[NPRIM], pr[NPRIM], f[NCONS];
