@@ -408,6 +408,11 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     // C) start on the slopes at once and the owner warps join when their cells are done.
     const int nwa = (pxs + pys + pzs) >> 5;
     for (int k = kb; k < ke; k++) {
+      if (own) {  // the cell's U is read in phase C, two phases from now: pull it into L2
+        const double* u0 = a.U + L.at(NCONS, 0, k + NGH, jj + NGH, ii + NGH);
+#pragma unroll
+        for (int m = 0; m < NCONS; m++) prefetch_l2(u0 + m * fsU);
+      }
       wait_plane(k + 2);
       const R *pk = plane(k), *pk1 = plane(k + 1), *pk2 = plane(k + 2);
       // ---- phase A: slopes ----
