@@ -15,7 +15,10 @@
 //     (mhd.cpp:1483-1506) into the other P buffer together with the ghost images the next step
 //     needs, and folds the next step's dt / c_h candidates (mhd.cpp:1542-1550, 1589-1601) into a
 //     block reduction; the lower z-face flux of its column stays in registers.
-// Work lists are padded per sub-list to whole warps so that no warp mixes two code paths.
+// The slope list is padded per direction to whole warps (no warp mixes two code paths) and handed
+// out per warp from a shared counter; the face list is one unpadded list over all directions,
+// each face read in its rotated frame by direction-generic code.  Masked-off lanes cost the FP64
+// pipe as much as active ones, so padding is paid for in full.
 // Step n reads dt and c_h from ctrl->slot[n%3] (made by step n-1 or by the initial reduction),
 // reduces into slot[(n+1)%3] and resets slot[(n+2)%3]; the last CTA to finish advances the step
 // counter and the simulated time.  All launches of a run are identical and can be captured once in
@@ -356,6 +359,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       if (!mbar_wait(&bars[s], (fills[s] - 1) & 1, &ctrl->status)) s_abort = 1;
     };
     auto PV = [&](const R* pl, int n, int i, int j) -> R { return pl[((j + 2) * NPRIM + n) * PX + (i + 2)]; };
+    auto PV0 = [&](const R* pl, int i, int j) -> const R& { return pl[((j + 2) * NPRIM) * PX + (i + 2)]; };
     auto SLX = [&](int n, int i, int j) -> R& { return slx[(n * TY + j) * (TX + 2) + (i + 1)]; };
     auto SLY = [&](int n, int i, int j) -> R& { return sly[(n * (TY + 2) + (j + 1)) * TX + i]; };
     auto SLZ = [&](int b, int n, int i, int j) -> R& { return slz[((b * NPRIM + n) * TY + j) * TX + i]; };
@@ -395,11 +399,10 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     }
     if (kb + 2 <= ke + 1) fills[slot_of(kb + 2)]++;
 
-    // work-list sizes (padded to whole warps per sub-list)
+    // work-list sizes (the slope sub-lists padded to whole warps)
     const int nxs = cy * (cx + 2), nys = (cy + 2) * cx, nzs = cy * cx;
     const int nxf = cy * (cx + 1), nyf = (cy + 1) * cx, nzf = cy * cx;
     const int pxs = (nxs + 31) & ~31, pys = (nys + 31) & ~31, pzs = (nzs + 31) & ~31;
-    const int pxf = (nxf + 31) & ~31, pyf = (nyf + 31) & ~31, pzf = (nzf + 31) & ~31;
 
     // Two barriers per plane.  Phase A writes only slope buffers that the previous plane's phase C
     // does not read, and phase C reads no ring plane, so neither the start nor the end of a plane
@@ -456,57 +459,77 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       __syncthreads();
       if (s_abort) break;  // a plane that never arrived (bounded wait): the data above is not used
       // ---- phase B: face fluxes (on the first plane also the faces kb-1/2, into slope buffer 2) ----
+      // One list over the x, y and z faces (and the lower z faces on the first plane) with no
+      // padding between directions: a thread reads its face's primitives and slopes in the rotated
+      // order (normal, first and second tangential components), forms the flux with the
+      // direction-generic code (Dir<0>) and stores it back into the unrotated slots.  Only the
+      // last warp of the list has idle lanes.
       if (tid == 0) s_aitem = 0;  // every warp has left phase A; the barrier after phase B publishes it
-      const int nq = pxf + pyf + (k == kb ? 2 * pzf : pzf);
-      for (int q = tid; q < nq; q += NT) {
-        R pl[NPRIM], pr[NPRIM], f[NCONS];
-        if (q < pxf) {
+      const int nfb = nxf + nyf + (k == kb ? 2 * nzf : nzf);
+      for (int q = tid; q < ((nfb + 31) & ~31); q += NT) {
+        if (q < nfb) {
+          int rot, sstr, fstr;        // rotation (0, 1, 2 = x, y, z); slope and flux slot strides
+          const R *pa, *pb, *sa, *sb;  // variable 0 of the left / right cell: primitive, slope
+          R* fo;                      // flux slot 0 of the face
           if (q < nxf) {
             const int j = q / (cx + 1), i = q % (cx + 1);
-#pragma unroll
-            for (int n = 0; n < NPRIM; n++) {
-              pl[n] = left_state(PV(pk, n, i - 1, j), SLX(n, i - 1, j));
-              pr[n] = right_state(PV(pk, n, i, j), SLX(n, i, j));
-            }
-            face_flux<R, 1>(pl, pr, glm, f, riemann);
-#pragma unroll
-            for (int m = 0; m < NCONS; m++) FXS(m, i, j) = f[m];
-          }
-        } else if (q < pxf + pyf) {
-          const int r = q - pxf;
-          if (r < nyf) {
+            rot = 0;
+            pa = &PV0(pk, i - 1, j);
+            pb = pa + 1;
+            sa = &SLX(0, i - 1, j);
+            sb = sa + 1;
+            sstr = TY * (TX + 2);
+            fo = &FXS(0, i, j);
+            fstr = TY * (TX + 1);
+          } else if (q < nxf + nyf) {
+            const int r = q - nxf, j = r / cx, i = r % cx;
+            rot = 1;
+            pa = &PV0(pk, i, j - 1);
+            pb = pa + NPRIM * PX;
+            sa = &SLY(0, i, j - 1);
+            sb = sa + TX;
+            sstr = (TY + 2) * TX;
+            fo = &FYS(0, i, j);
+            fstr = (TY + 1) * TX;
+          } else {
+            int r = q - nxf - nyf;
+            const bool lower = r >= nzf;  // face kb-1/2 (first plane only)
+            if (lower) r -= nzf;
             const int j = r / cx, i = r % cx;
-#pragma unroll
-            for (int n = 0; n < NPRIM; n++) {
-              pl[n] = left_state(PV(pk, n, i, j - 1), SLY(n, i, j - 1));
-              pr[n] = right_state(PV(pk, n, i, j), SLY(n, i, j));
-            }
-            face_flux<R, 2>(pl, pr, glm, f, riemann);
-#pragma unroll
-            for (int m = 0; m < NCONS; m++) FYS(m, i, j) = f[m];
-          }
-        } else {
-          int r = q - pxf - pyf;
-          const bool lower = r >= pzf;  // face kb-1/2 (first plane only)
-          if (lower) r -= pzf;
-          if (r < nzf) {
-            const int j = r / cx, i = r % cx;
-            const R* pa = lower ? plane(kb - 1) : pk;
-            const R* pb = lower ? pk : pk1;
-            const int sa = lower ? 2 : zb, sb = lower ? zb : (zb ^ 1);
-#pragma unroll
-            for (int n = 0; n < NPRIM; n++) {
-              pl[n] = left_state(PV(pa, n, i, j), SLZ(sa, n, i, j));
-              pr[n] = right_state(PV(pb, n, i, j), SLZ(sb, n, i, j));
-            }
-            face_flux<R, 3>(pl, pr, glm, f, riemann);
+            rot = 2;
+            pa = &PV0(lower ? plane(kb - 1) : pk, i, j);
+            pb = &PV0(lower ? pk : pk1, i, j);
+            sa = &SLZ(lower ? 2 : zb, 0, i, j);
+            sb = &SLZ(lower ? zb : (zb ^ 1), 0, i, j);
+            sstr = TY * TX;
             // the lower face overwrites the slopes it alone read (column (i, j) of buffer 2)
-#pragma unroll
-            for (int m = 0; m < NCONS; m++) {
-              if (lower) SLZ(2, m, i, j) = f[m];
-              else FZS(m, i, j) = f[m];
-            }
+            fo = lower ? &SLZ(2, 0, i, j) : &FZS(0, i, j);
+            fstr = TY * TX;
           }
+          const int c1 = unrot_comp(1, rot), c2 = unrot_comp(2, rot);
+          // unrotated variable read into rotated slot n (n is a constant after unrolling)
+          auto var_of = [&](int n) {
+            if (n == nve1 || n == nbm1) return n + rot;
+            if (n == nve2 || n == nbm2) return n - 1 + c1;
+            if (n == nve3 || n == nbm3) return n - 2 + c2;
+            return n;
+          };
+          R pl[NPRIM], pr[NPRIM], f[NCONS];
+#pragma unroll
+          for (int n = 0; n < NPRIM; n++) {
+            const int v = var_of(n);
+            pl[n] = left_state(pa[v * PX], sa[v * sstr]);
+            pr[n] = right_state(pb[v * PX], sb[v * sstr]);
+          }
+          face_flux<R, 0>(pl, pr, glm, f, riemann, rot);
+          auto slot_of_flux = [&](int m) {
+            if (m == mrv1 || m == mbm1) return m + rot;
+            if (m == mrv2 || m == mbm2) return m - 1 + c1;
+            if (m == mrv3 || m == mbm3) return m - 2 + c2;
+            return m;
+          };
+#pragma unroll
+          for (int m = 0; m < NCONS; m++) fo[slot_of_flux(m) * fstr] = f[m];
         }
       }
       __syncthreads();  // faces formed; plane k (and on the first plane kb-1) read for the last time

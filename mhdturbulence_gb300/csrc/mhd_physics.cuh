@@ -216,14 +216,38 @@ template <> struct Dir<3> {
   static constexpr int ob_a = mbm1, sb_a = mubv, ob_b = mbm2, sb_b = mubw;
 };
 
+// Dir<0>: the face's primitives arrive rotated already (normal, first and second tangential
+// components in the slots of x, y, z, as Dir<1> reads them), for the fused step's direction-generic
+// face list.  rot = 0, 1, 2 for x, y, z faces; the one place it enters the arithmetic is the sums
+// over the three components, which keep the unrotated x, y, z order (sum_sq3), so a Dir<0> flux is
+// bit for bit the Dir<1/2/3> flux of the same face.
+template <> struct Dir<0> : Dir<1> {};
+
+// Unrotated component (0, 1, 2 = x, y, z) held in rotated slot 0, 1, 2 of a face with rotation rot.
+__device__ __forceinline__ int unrot_comp(int slot, int rot) { return slot + rot < 3 ? slot + rot : slot + rot - 3; }
+
+// P[b]^2 + P[b+1]^2 + P[b+2]^2 over unrotated components x, y, z in that order.
+template <int DIR, class R>
+__device__ __forceinline__ R sum_sq3(const R (&P)[NPRIM], int b, int rot) {
+  if constexpr (DIR != 0) {
+    return P[b] * P[b] + P[b + 1] * P[b + 1] + P[b + 2] * P[b + 2];
+  } else {
+    const R r0 = P[b], r1 = P[b + 1], r2 = P[b + 2];
+    const R x = rot == 0 ? r0 : (rot == 1 ? r2 : r1);
+    const R y = rot == 0 ? r1 : (rot == 1 ? r0 : r2);
+    const R z = rot == 0 ? r2 : (rot == 1 ? r1 : r0);
+    return x * x + y * y + z * z;
+  }
+}
+
 // Prim2ConsD, mhd.cpp:997-1076 (note the energy flux term bsq*B_d of mhd.cpp:1049-1050).
 template <class R, int DIR>
-__device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
+__device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC], int rot = 0) {
   using D = Dir<DIR>;
   const R rho = Prim[nden];
   const R rhoinv = fdiv_est(R(1), rho);  // only in the fast-speed estimate below
-  const R vsq = Prim[nve1] * Prim[nve1] + Prim[nve2] * Prim[nve2] + Prim[nve3] * Prim[nve3];
-  const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
+  const R vsq = sum_sq3<DIR>(Prim, nve1, rot);
+  const R bsq = sum_sq3<DIR>(Prim, nbm1, rot);
   Cons[mudn] = rho;
   Cons[D::muv1] = rho * Prim[nve1];
   Cons[D::muv2] = rho * Prim[nve2];
@@ -257,12 +281,12 @@ __device__ __forceinline__ void prim2cons(const R (&Prim)[NPRIM], R (&Cons)[NVEC
 // upwind side only: the state part (conserved variables, fast speed, normal velocity, total
 // pressure) for both sides, then the flux part for the chosen side, with prim2cons's expressions.
 template <class R, int DIR>
-__device__ __forceinline__ void prim2cons_state(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
+__device__ __forceinline__ void prim2cons_state(const R (&Prim)[NPRIM], R (&Cons)[NVEC], int rot = 0) {
   using D = Dir<DIR>;
   const R rho = Prim[nden];
   const R rhoinv = fdiv_est(R(1), rho);
-  const R vsq = Prim[nve1] * Prim[nve1] + Prim[nve2] * Prim[nve2] + Prim[nve3] * Prim[nve3];
-  const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
+  const R vsq = sum_sq3<DIR>(Prim, nve1, rot);
+  const R bsq = sum_sq3<DIR>(Prim, nbm1, rot);
   Cons[mudn] = rho;
   Cons[D::muv1] = rho * Prim[nve1];
   Cons[D::muv2] = rho * Prim[nve2];
@@ -281,10 +305,10 @@ __device__ __forceinline__ void prim2cons_state(const R (&Prim)[NPRIM], R (&Cons
 }
 // The flux slots (mfdn .. mfst) of Cons from the primitive state and Cons[muet], Cons[mpre].
 template <class R, int DIR>
-__device__ __forceinline__ void prim2cons_flux(const R (&Prim)[NPRIM], R (&Cons)[NVEC]) {
+__device__ __forceinline__ void prim2cons_flux(const R (&Prim)[NPRIM], R (&Cons)[NVEC], int rot = 0) {
   using D = Dir<DIR>;
   const R rho = Prim[nden];
-  const R bsq = Prim[nbm1] * Prim[nbm1] + Prim[nbm2] * Prim[nbm2] + Prim[nbm3] * Prim[nbm3];
+  const R bsq = sum_sq3<DIR>(Prim, nbm1, rot);
   const R ptl = Cons[mpre];
   Cons[mfdn] = rho * Prim[D::nved];
   Cons[D::mfv1] = rho * Prim[nve1] * Prim[D::nved] - Prim[nbm1] * Prim[D::nbmd];
@@ -456,7 +480,7 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
 // Results agree with hlld() to rounding (and in the sign of zero results).
 template <class R, int DIR>
 __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], const R (&Pl)[NPRIM],
-                                            const R (&Pr)[NPRIM], R (&nflux)[NCONS]) {
+                                            const R (&Pr)[NPRIM], R (&nflux)[NCONS], int rot = 0) {
   using D = Dir<DIR>;
   const R eps = R(1.0e-30);
   const R rol = leftst[mudn], eel = leftst[muet];
@@ -581,7 +605,7 @@ __device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&r
   R pup[NPRIM];
 #pragma unroll
   for (int n = 0; n < NPRIM; n++) pup[n] = left ? Pl[n] : Pr[n];
-  prim2cons_flux<R, DIR>(pup, cst);
+  prim2cons_flux<R, DIR>(pup, cst, rot);
   const R rx = cst[muvu], ry = cst[muvv], rz = cst[muvw];
   nflux[mden] = cst[mfdn] + (rost - ro) * ms;
   nflux[meto] = cst[mfet] + (eest - ee) * ms + (eedst - eest) * msst;
@@ -688,26 +712,28 @@ template <class R>
 __device__ __forceinline__ GlmConst<R> glm_const(R chg) {
   return GlmConst<R>{chg, fdiv(R(0.5), chg), chg * chg};
 }
+// DIR = 0: rotated primitives (see Dir<0>) and F in the rotated order of Dir<1> (normal, first and
+// second tangential momentum and field fluxes); the caller puts them back in their slots.
 template <class R, int DIR>
 __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NPRIM], const GlmConst<R>& g,
-                                          R (&F)[NCONS], int riemann = RIEMANN_HLLD) {
+                                          R (&F)[NCONS], int riemann = RIEMANN_HLLD, int rot = 0) {
   const R chg = g.chg;
   using D = Dir<DIR>;
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
   constexpr bool branch_hlld = kFast;
   if (branch_hlld && riemann == RIEMANN_HLLD) {  // the upwind flux is formed inside hlld_branch
-    prim2cons_state<R, DIR>(Pl, Cl);
-    prim2cons_state<R, DIR>(Pr, Cr);
+    prim2cons_state<R, DIR>(Pl, Cl, rot);
+    prim2cons_state<R, DIR>(Pr, Cr, rot);
   } else {
-    prim2cons<R, DIR>(Pl, Cl);
-    prim2cons<R, DIR>(Pr, Cr);
+    prim2cons<R, DIR>(Pl, Cl, rot);
+    prim2cons<R, DIR>(Pr, Cr, rot);
   }
   if (riemann == RIEMANN_HLLE) {
     hlle<R, DIR>(Cl, Cr, nf);
   } else if (riemann == RIEMANN_HLLC) {
     hllc<R, DIR>(Cl, Cr, Pl, Pr, nf);
   } else {
-    if constexpr (branch_hlld) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf);
+    if constexpr (branch_hlld) hlld_branch<R, DIR>(Cl, Cr, Pl, Pr, nf, rot);
     else hlld<R, DIR>(Cl, Cr, Pl, Pr, nf);
   }
   F[mden] = nf[mden];
