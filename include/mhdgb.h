@@ -165,7 +165,11 @@ int mhdgb_sync(mhdgb_solver* h, mhdgb_report* report);
 int mhdgb_reset_clock(mhdgb_solver* h);
 /* One step on caller-owned host arrays: upload U (10 fields, reference layout), run nsteps fused
  * steps, download the new U and return the step's dt and c_h.  The drop-in form of the loop body
- * for callers that keep the state on the host. */
+ * for callers that keep the state on the host.  Page-locked, mapped arrays (cudaHostAlloc,
+ * cudaHostRegister, a pinned torch tensor) are read and written by the kernels themselves over the
+ * host link: the recovery pass reads U_in, the last step writes each updated cell of U_out, and the
+ * ghost cells of a separate U_out are copied from U_in.  Other arrays go through a device staging
+ * buffer.  Both give the same U_out bit for bit; U_out may be U_in. */
 int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nsteps, double* dt, double* chg);
 
 /* Time nsteps fused steps with CUDA events recorded on the handle's stream around the enqueued

@@ -64,8 +64,9 @@ int variants_fp64(const FusedVariant** out) {
   return (int)(sizeof(v) / sizeof(v[0])) - 1;  // the last entry is the run-time solver kernel
 }
 
-cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
-  return v_fast64::recover_launch<double>(a, which, slot, nsm, s);
+cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
+                         double* uh_ghost_out) {
+  return v_fast64::recover_launch<double>(a, which, slot, nsm, s, uh_in, uh_ghost_out);
 }
 
 }  // namespace detail

@@ -570,6 +570,12 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         update_cell(acc, a.U + c0, fsU, dt, chd, dtf, chf, a, ii + NGH, jj + NGH, k + NGH, u);
 #pragma unroll
         for (int m = 0; m < NCONS; m++) a.U[c0 + m * fsU] = u[m];
+        if (a.Uh) {  // the caller's host copy of U (end-to-end steps), field stride itot
+          double* uh = a.Uh + ((size_t)(ii + NGH) + (size_t)L.itot * NCONS * ((size_t)(jj + NGH) +
+                                                                            (size_t)L.jtot * (size_t)(k + NGH)));
+#pragma unroll
+          for (int m = 0; m < NCONS; m++) uh[(size_t)m * L.itot] = u[m];
+        }
         R dtc, chc;
         recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, k, spacing_of<R>(a, 0, ii + NGH),
                         spacing_of<R>(a, 1, jj + NGH), spacing_of<R>(a, 2, k + NGH), dtc, chc, bad);
@@ -615,26 +621,55 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
   }
 }
 
-// Recovery of P from U for the interior (+ ghost images) and the dt/c_h reduction into a slot:
-// the state a fused run starts from.
+// Recovery of P from U for the interior (+ ghost images) and the dt/c_h reduction into slot: the
+// state a fused run starts from.  uh_in null: from the device U.  Otherwise the state comes from the caller's
+// host array (reference layout, itot x jtot x ktot, over the host link): every cell is copied into
+// the device U on the way, interior cells are recovered, and ghost cells also go to uh_ghost_out
+// when it is given (an output array other than the input).
 template <class R>
-__global__ void k_recover(FusedArgs a, int which, RedSlot* slot) {
+__global__ void k_recover(FusedArgs a, int which, RedSlot* slot, const double* __restrict__ uh_in,
+                          double* __restrict__ uh_ghost_out) {
   __shared__ double scratch[64];
   const Layout L = a.L;
-  const long long n = (long long)L.nx * L.ny * L.nz;
   R mn = R(1e30), mx = R(0);
   unsigned bad = 0;
   R* Pout = reinterpret_cast<R*>(a.P[which]);
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int ii = (int)(t % L.nx), jj = (int)((t / L.nx) % L.ny), kk = (int)(t / ((long long)L.nx * L.ny));
-    double u[NCONS];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (!uh_in) {
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+      const int ii = (int)(t % L.nx), jj = (int)((t / L.nx) % L.ny), kk = (int)(t / ((long long)L.nx * L.ny));
+      double u[NCONS];
 #pragma unroll
-    for (int m = 0; m < NCONS; m++) u[m] = a.U[L.at(NCONS, m, kk + NGH, jj + NGH, ii + NGH)];
-    R dtc, chc;
-    recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, kk, spacing_of<R>(a, 0, ii + NGH), spacing_of<R>(a, 1, jj + NGH),
-                    spacing_of<R>(a, 2, kk + NGH), dtc, chc, bad);
-    mn = smin(mn, dtc);
-    mx = smax(mx, chc);
+      for (int m = 0; m < NCONS; m++) u[m] = a.U[L.at(NCONS, m, kk + NGH, jj + NGH, ii + NGH)];
+      R dtc, chc;
+      recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, kk, spacing_of<R>(a, 0, ii + NGH),
+                      spacing_of<R>(a, 1, jj + NGH), spacing_of<R>(a, 2, kk + NGH), dtc, chc, bad);
+      mn = smin(mn, dtc);
+      mx = smax(mx, chc);
+    }
+  } else {
+    const long long n = (long long)L.itot * L.jtot * L.ktot;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+      const int i = (int)(t % L.itot), j = (int)((t / L.itot) % L.jtot), k = (int)(t / ((long long)L.itot * L.jtot));
+      const size_t h0 = (size_t)i + (size_t)L.itot * NCONS * ((size_t)j + (size_t)L.jtot * (size_t)k);
+      double u[NCONS];
+#pragma unroll
+      for (int m = 0; m < NCONS; m++) u[m] = uh_in[h0 + (size_t)m * L.itot];
+#pragma unroll
+      for (int m = 0; m < NCONS; m++) a.U[L.at(NCONS, m, k, j, i)] = u[m];
+      const int ii = i - NGH, jj = j - NGH, kk = k - NGH;
+      if ((unsigned)ii < (unsigned)L.nx && (unsigned)jj < (unsigned)L.ny && (unsigned)kk < (unsigned)L.nz) {
+        R dtc, chc;
+        recover_cell<R>(u, a.gam, Pout, L, a.bc, ii, jj, kk, spacing_of<R>(a, 0, i), spacing_of<R>(a, 1, j),
+                        spacing_of<R>(a, 2, k), dtc, chc, bad);
+        mn = smin(mn, dtc);
+        mx = smax(mx, chc);
+      } else if (uh_ghost_out) {
+#pragma unroll
+        for (int m = 0; m < NCONS; m++) uh_ghost_out[h0 + (size_t)m * L.itot] = u[m];
+      }
+    }
   }
   if (bad) atomicOr(&a.ctrl->status, bad);
   block_reduce_to_slot((double)mn, (double)mx, scratch, slot);
@@ -665,12 +700,13 @@ struct FusedLauncher {
 };
 
 template <class R>
-cudaError_t recover_launch(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
+cudaError_t recover_launch(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s,
+                           const double* uh_in, double* uh_ghost_out) {
   const int bs = 256;
-  const long long n = (long long)a.L.nx * a.L.ny * a.L.nz;
+  const long long n = uh_in ? (long long)a.L.itot * a.L.jtot * a.L.ktot : (long long)a.L.nx * a.L.ny * a.L.nz;
   long long g = (n + bs - 1) / bs;
   if (g > (long long)nsm * 8) g = (long long)nsm * 8;
-  k_recover<R><<<(unsigned)g, bs, 0, s>>>(a, which, slot);
+  k_recover<R><<<(unsigned)g, bs, 0, s>>>(a, which, slot, uh_in, uh_ghost_out);
   return cudaGetLastError();
 }
 

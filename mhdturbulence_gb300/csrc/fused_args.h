@@ -30,6 +30,9 @@ struct FusedArgs {
   int riemann;                         // RIEMANN_HLLD / _HLLE / _HLLC
   int ntx, nty, nkc, kc;               // tiles in x, y; chunks in z; planes per chunk
   Ctrl* ctrl;
+  // End-to-end steps: the caller's host array of U (reference layout, itot x jtot x ktot, reached
+  // over the host link), written by the step's cell updates besides U; null otherwise.
+  double* Uh;
 };
 
 // One grid of a launch: its arguments, the TMA maps of its two primitive buffers and its range of

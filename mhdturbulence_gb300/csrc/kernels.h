@@ -36,15 +36,19 @@ cudaError_t launch_snapshot(const double* U, const double* P, const Layout& L, d
 int fused_variants(FusedKind kind, const FusedVariant** out);
 // Recover P (FP64 for FP64 kinds, FP32 for mixed) + ghost images from a.U into a.P[which];
 // reduce dt/c_h into slot.
-cudaError_t launch_recover(FusedKind kind, const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
+cudaError_t launch_recover(FusedKind kind, const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s,
+                           const double* uh_in = nullptr, double* uh_ghost_out = nullptr);
 
 namespace detail {
 int variants_exact(const FusedVariant** out);
 int variants_fp64(const FusedVariant** out);
 int variants_mixed(const FusedVariant** out);
-cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
-cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
-cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s);
+cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
+                          double* uh_ghost_out);
+cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
+                          double* uh_ghost_out);
+cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
+                          double* uh_ghost_out);
 cudaError_t fdiv_selftest(int n, unsigned long long seed, unsigned long long* d_max_ulp, cudaStream_t s);
 }  // namespace detail
 

@@ -25,8 +25,9 @@ int variants_mixed(const FusedVariant** out) {
   return (int)(sizeof(v) / sizeof(v[0])) - 1;  // the last entry is the run-time solver kernel
 }
 
-cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
-  return v_mixed::recover_launch<float>(a, which, slot, nsm, s);
+cudaError_t recover_mixed(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
+                          double* uh_ghost_out) {
+  return v_mixed::recover_launch<float>(a, which, slot, nsm, s, uh_in, uh_ghost_out);
 }
 
 }  // namespace detail

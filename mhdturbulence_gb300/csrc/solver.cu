@@ -89,6 +89,9 @@ __global__ void k_ctrl_restore(Ctrl* c, unsigned long long step, double time, do
   c->work_next = 0;
 }
 
+// Point the step's host copy of U at v (null: none), in the launch descriptor on the device.
+__global__ void k_set_host_u(InstanceDesc* d, double* v) { d->a.Uh = v; }
+
 __global__ void k_ctrl_set_stop(Ctrl* c, double tmax, unsigned long long max_step) {
   c->tmax = tmax;
   c->max_step = max_step;
@@ -1024,15 +1027,75 @@ int mhdgb_reset_clock(mhdgb_solver* h) {
   return MHDGB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device address of a host array of n doubles that is page-locked and mapped (cudaHostAlloc,
+// cudaHostRegister), or null.  Both ends are checked, so a registration that covers only part of
+// the array is not taken.
+const double* mapped_view(const double* p, size_t n) {
+  cudaPointerAttributes a0{}, a1{};
+  if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, p + n - 1) != cudaSuccess) {
+    cudaGetLastError();  // an unknown pointer is not an error here
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  const double* d0 = static_cast<const double*>(a0.devicePointer);
+  if (static_cast<const double*>(a1.devicePointer) != d0 + (n - 1)) return nullptr;
+  return d0;
+}
+
+// mhdgb_step_host with page-locked, mapped arrays: the recovery pass reads U_in over the host link
+// (copying every cell into the device U and, for a separate U_out, the ghost cells into U_out), and
+// the last step's cell updates write U_out as they are made, so the transfers overlap the work and
+// no staging copy or repacking pass runs.
+int step_host_mapped(mhdgb_solver* h, const double* din, double* dout, bool same, int nsteps) {
+  Ctrl c;
+  int rc = read_ctrl(h, &c);
+  if (rc) return rc;
+  h->cur_step = (long long)c.step;
+  h->have_state = true;
+  h->p_user = false;
+  CK(h, launch_reset_slot(&h->ctrl->slot[c.step % 3], h->stream));
+  CK(h, launch_reset_slot(&h->ctrl->slot[(c.step + 1) % 3], h->stream));
+  const FusedArgs a = fused_args(h);
+  CK(h, launch_recover(h->kind, a, cur_index(h), &h->ctrl->slot[c.step % 3], h->nsm, h->stream, din,
+                       same ? nullptr : dout));
+  h->prepared = true;
+  h->p64_valid = h->kind != FUSED_MIXED;
+  if (nsteps > 1 && (rc = mhdgb_step(h, nsteps - 1))) return rc;
+  k_set_host_u<<<1, 1, 0, h->stream>>>(h->d_desc, dout);
+  CK(h, cudaGetLastError());
+  rc = mhdgb_step(h, 1);
+  k_set_host_u<<<1, 1, 0, h->stream>>>(h->d_desc, nullptr);
+  CK(h, cudaGetLastError());
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nsteps, double* dt, double* chg) {
   if (!h || !U_in || !U_out || nsteps < 1) return MHDGB_ERR_ARG;
   int rc = set_device(h);
-  if (rc || (rc = settle(h)) || (rc = upload_u(h, U_in))) return rc;
-  h->have_state = true;
-  h->prepared = false;
-  h->p_user = false;
-  if ((rc = mhdgb_prepare(h)) || (rc = mhdgb_step(h, nsteps))) return rc;
-  if ((rc = settle(h)) || (rc = download_u(h, U_out))) return rc;
+  if (rc) return rc;
+  const Layout& L = h->L;
+  const size_t n = (size_t)NCONS * L.itot * L.jtot * L.ktot;
+  const double* din = mapped_view(U_in, n);
+  const double* dout = mapped_view(U_out, n);
+  if (din && dout) {
+    if ((rc = step_host_mapped(h, din, const_cast<double*>(dout), din == dout, nsteps))) return rc;
+  } else {
+    if ((rc = settle(h)) || (rc = upload_u(h, U_in))) return rc;
+    h->have_state = true;
+    h->prepared = false;
+    h->p_user = false;
+    if ((rc = mhdgb_prepare(h)) || (rc = mhdgb_step(h, nsteps))) return rc;
+    if ((rc = settle(h)) || (rc = download_u(h, U_out))) return rc;
+  }
   mhdgb_report rep;
   rc = mhdgb_sync(h, &rep);
   if (dt) *dt = rep.dt;

@@ -355,8 +355,9 @@ int variants_exact(const FusedVariant** out) {
   *out = v;
   return (int)(sizeof(v) / sizeof(v[0])) - 1;  // the last entry is the run-time solver kernel
 }
-cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
-  return v_exact::recover_launch<double>(a, which, slot, nsm, s);
+cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
+                          double* uh_ghost_out) {
+  return v_exact::recover_launch<double>(a, which, slot, nsm, s, uh_in, uh_ghost_out);
 }
 }  // namespace detail
 
@@ -368,11 +369,12 @@ int fused_variants(FusedKind kind, const FusedVariant** out) {
   }
 }
 
-cudaError_t launch_recover(FusedKind kind, const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s) {
+cudaError_t launch_recover(FusedKind kind, const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s,
+                           const double* uh_in, double* uh_ghost_out) {
   switch (kind) {
-    case FUSED_FP64_EXACT: return detail::recover_exact(a, which, slot, nsm, s);
-    case FUSED_FP64: return detail::recover_fp64(a, which, slot, nsm, s);
-    default: return detail::recover_mixed(a, which, slot, nsm, s);
+    case FUSED_FP64_EXACT: return detail::recover_exact(a, which, slot, nsm, s, uh_in, uh_ghost_out);
+    case FUSED_FP64: return detail::recover_fp64(a, which, slot, nsm, s, uh_in, uh_ghost_out);
+    default: return detail::recover_mixed(a, which, slot, nsm, s, uh_in, uh_ghost_out);
   }
 }
 
