@@ -185,6 +185,14 @@ __device__ __forceinline__ void tma_load_4d(void* smem_dst, const CUtensorMap* m
       : "memory");
 }
 
+// Division by a run-time divisor d that stays fixed over many numerators: q / d as the high half
+// of 2q * ceil(2^31 / d), exact whenever q * d < 2^31 (the work-list decode has q, d < 2^15).
+struct FastDiv {
+  unsigned d, m;
+  __device__ __forceinline__ explicit FastDiv(int d_) : d((unsigned)d_), m((0x80000000u + (unsigned)d_ - 1u) / (unsigned)d_) {}
+  __device__ __forceinline__ int div(int q) const { return (int)__umulhi((unsigned)q << 1, m); }
+};
+
 __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }

@@ -399,7 +399,8 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     }
     if (kb + 2 <= ke + 1) fills[slot_of(kb + 2)]++;
 
-    // work-list sizes (the slope sub-lists padded to whole warps)
+    // work-list sizes (the slope sub-lists padded to whole warps) and the divisors of their decode
+    const FastDiv dv0(cx), dv1(cx + 1), dv2(cx + 2);
     const int nxs = cy * (cx + 2), nys = (cy + 2) * cx, nzs = cy * cx;
     const int nxf = cy * (cx + 1), nyf = (cy + 1) * cx, nzf = cy * cx;
     const int pxs = (nxs + 31) & ~31, pys = (nys + 31) & ~31, pzs = (nzs + 31) & ~31;
@@ -427,7 +428,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         const int q = (w << 5) | (tid & 31);
         if (q < pxs) {
           if (q < nxs) {
-            const int j = q / (cx + 2), i = q % (cx + 2) - 1;
+            const int j = dv2.div(q), i = q - j * (cx + 2) - 1;
 #pragma unroll
             for (int n = 0; n < NPRIM; n++) {
               const R m1 = PV(pk, n, i - 1, j), c0 = PV(pk, n, i, j), p1 = PV(pk, n, i + 1, j);
@@ -437,7 +438,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         } else if (q < pxs + pys) {
           const int r = q - pxs;
           if (r < nys) {
-            const int j = r / cx - 1, i = r % cx;
+            const int jr = dv0.div(r), j = jr - 1, i = r - jr * cx;
 #pragma unroll
             for (int n = 0; n < NPRIM; n++) {
               const R m1 = PV(pk, n, i, j - 1), c0 = PV(pk, n, i, j), p1 = PV(pk, n, i, j + 1);
@@ -447,7 +448,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
         } else {
           const int r = q - pxs - pys;
           if (r < nzs) {
-            const int j = r / cx, i = r % cx;
+            const int j = dv0.div(r), i = r - j * cx;
 #pragma unroll
             for (int n = 0; n < NPRIM; n++) {
               const R c0 = PV(pk, n, i, j), c1 = PV(pk1, n, i, j), c2 = PV(pk2, n, i, j);
@@ -472,7 +473,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
           const R *pa, *pb, *sa, *sb;  // variable 0 of the left / right cell: primitive, slope
           R* fo;                      // flux slot 0 of the face
           if (q < nxf) {
-            const int j = q / (cx + 1), i = q % (cx + 1);
+            const int j = dv1.div(q), i = q - j * (cx + 1);
             rot = 0;
             pa = &PV0(pk, i - 1, j);
             pb = pa + 1;
@@ -482,7 +483,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
             fo = &FXS(0, i, j);
             fstr = TY * (TX + 1);
           } else if (q < nxf + nyf) {
-            const int r = q - nxf, j = r / cx, i = r % cx;
+            const int r = q - nxf, j = dv0.div(r), i = r - j * cx;
             rot = 1;
             pa = &PV0(pk, i, j - 1);
             pb = pa + NPRIM * PX;
@@ -495,7 +496,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
             int r = q - nxf - nyf;
             const bool lower = r >= nzf;  // face kb-1/2 (first plane only)
             if (lower) r -= nzf;
-            const int j = r / cx, i = r % cx;
+            const int j = dv0.div(r), i = r - j * cx;
             rot = 2;
             pa = &PV0(lower ? plane(kb - 1) : pk, i, j);
             pb = &PV0(lower ? pk : pk1, i, j);
