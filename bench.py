@@ -330,6 +330,12 @@ def run_ours(args, ws, rank, local):
             inst = prof["fp64_pipe_inst_per_cell"] * cells / (ms_step * 1e-3) / 1e9
             fp64_pipe["inst_frac"] = inst / (fp64_rate / 2.0)
             fp64_pipe["pipe_active_ncu"] = prof.get("fp64_pipe_active_ncu")
+        # the reference algorithm's own operation count (each add, mul, div, sqrt one flop), counted
+        # on the oracle restatement with an instrumented double: the work rate in its terms
+        ref_ops = profile_summary("flops_per_cell_oracle.json")
+        if ref_ops and ref_ops.get("flops_per_cell"):
+            fp64_pipe["reference_flops_per_cell"] = ref_ops["flops_per_cell"]
+            fp64_pipe["reference_gflops"] = ref_ops["flops_per_cell"] * cells / (ms_step * 1e-3) / 1e9
     mx = res["mixed"]
     mx_step = mx["ms"] / mx["steps"]
     mx_value = replica_value(ws, cells, mx["steps"], mx["ms"])

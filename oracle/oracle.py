@@ -127,3 +127,29 @@ def set_threads(n: int) -> None:
 
 def get_threads() -> int:
     return lib().orc_get_threads()
+
+
+FLOPCOUNT_PATH = os.path.join(HERE, "_build", "flopcount")
+
+
+def count_ops(U0, nx, ny, nz, domain, bc, gam=5.0 / 3.0, cfl=0.05, spacing_quirk=False, riemann=0, nsteps=1):
+    """Operations per cell-update of the solver step, counted by running the restatement with an
+    operation-counting double (oracle/flopcount.cpp): step 1 by stage, and the average over nsteps.
+    Returns (counts, U after nsteps); the state equals the plain oracle's bit for bit."""
+    import json
+    import tempfile
+    if not os.path.exists(FLOPCOUNT_PATH) or \
+            os.path.getmtime(FLOPCOUNT_PATH) < os.path.getmtime(os.path.join(HERE, "mhd_oracle.c")) or \
+            os.path.getmtime(FLOPCOUNT_PATH) < os.path.getmtime(os.path.join(HERE, "flopcount.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "flopcount"], check=True)
+    U0 = np.ascontiguousarray(U0, dtype=np.float64)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "u0.bin"), os.path.join(d, "u1.bin")
+        U0.tofile(fin)
+        (x0, x1), (y0, y1), (z0, z1) = domain
+        args = [FLOPCOUNT_PATH, nx, ny, nz, repr(float(gam)), repr(float(cfl)), *bc, int(bool(spacing_quirk)),
+                riemann, repr(float(x0)), repr(float(x1)), repr(float(y0)), repr(float(y1)), repr(float(z0)),
+                repr(float(z1)), fin, nsteps, fout]
+        r = subprocess.run([str(a) for a in args], check=True, capture_output=True, text=True)
+        U = np.fromfile(fout, dtype=np.float64).reshape(U0.shape)
+    return json.loads(r.stdout), U
