@@ -1086,7 +1086,10 @@ int mhdgb_step_host(mhdgb_solver* h, const double* U_in, double* U_out, int nste
   const size_t n = (size_t)NCONS * L.itot * L.jtot * L.ktot;
   const double* din = mapped_view(U_in, n);
   const double* dout = mapped_view(U_out, n);
-  if (din && dout) {
+  // arrays that overlap without being the same one take the staged route: the recovery pass writes
+  // U_out's ghost cells while it is still reading U_in
+  const bool partial_overlap = U_in != U_out && U_in < U_out + n && U_out < U_in + n;
+  if (din && dout && !partial_overlap) {
     if ((rc = step_host_mapped(h, din, const_cast<double*>(dout), din == dout, nsteps))) return rc;
   } else {
     if ((rc = settle(h)) || (rc = upload_u(h, U_in))) return rc;

@@ -57,3 +57,17 @@ def test_ghost_cells_of_a_separate_output_are_the_inputs():
         src, dst = _pinned(U0), _pinned(np.zeros_like(U0))
         s.step_host(src.numpy(), dst.numpy(), 1)
         assert np.array_equal(dst.numpy()[..., 0], U0[..., 0])
+
+
+def test_overlapping_arrays_give_the_same_state():
+    with Solver(NX, NY, NZ) as s:
+        s.init_kh(seed=5)
+        U0 = s.download_cons()
+        ref = np.empty_like(U0)
+        s.step_host(U0.copy(), ref, 1)
+        n, k = U0.size, 1000
+        buf = torch.empty(n + k, dtype=torch.float64, pin_memory=True)
+        b = buf.numpy()
+        b[:n] = U0.ravel()
+        s.step_host(b[:n].reshape(U0.shape), b[k:k + n].reshape(U0.shape), 1)
+        assert np.array_equal(b[k:k + n].reshape(U0.shape), ref)
