@@ -3,7 +3,9 @@
 // A handle owns, on its device: the conserved state U (FP64), two primitive buffers per precision
 // (the fused step reads one and writes the other), the three face-flux arrays and the pack buffers
 // of the stage path, the per-axis spacing tables, and the control block (Ctrl).  All arrays use
-// the reference FieldArray layout with a padded i pitch; host transfers are 2-D pitched copies.
+// the reference FieldArray layout with a padded i pitch.  Host arrays (dense rows of itot) move
+// through a device staging buffer and a row-repacking kernel; page-locked host arrays given to
+// mhdgb_step_host are instead read and written by the kernels themselves over the host link.
 #include <cudaTypedefs.h>
 
 #include <algorithm>
