@@ -196,6 +196,11 @@ int mhdgb_measure_fp64_rate(int device, double* gflops);
  * square root) against IEEE division and square root on n random operands; *max_ulp receives the
  * largest difference in units in the last place. */
 int mhdgb_selftest_division(int device, int n, unsigned long long seed, double* max_ulp);
+/* Self-test of failure detection (no reference counterpart): a kernel waits on a shared-memory
+ * barrier that nothing completes; the bounded wait the fused step uses for its plane loads gives
+ * up after about 2 s and returns with the timeout bit (4) set in *status, leaving the context
+ * usable.  *seconds receives the kernel's duration.  Nothing faults or hangs. */
+int mhdgb_selftest_wait_timeout(int device, double* seconds, unsigned* status);
 
 /* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):
  * out = {volume, <X(1-X)>, sqrt(<v_y^2>)} over the interior, FP64 sums. */

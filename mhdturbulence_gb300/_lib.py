@@ -88,6 +88,7 @@ SIGNATURES = {
     "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mhdgb_measure_fp64_rate": (C.c_int, [C.c_int, _dp]),
     "mhdgb_selftest_division": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, _dp]),
+    "mhdgb_selftest_wait_timeout": (C.c_int, [C.c_int, _dp, C.POINTER(C.c_uint)]),
     "mhdgb_diag": (C.c_int, [_vp, _dp]),
     "mhdgb_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double]),

@@ -165,10 +165,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return ok != 0;
 }
 
-// Returns false (and flags ST_TIMEOUT) if the phase did not complete within the spin budget.
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Every wait of a kernel on an mbarrier gives up after this long (or after kWaitMaxSpins polls,
+// whichever comes first), so a copy that never lands ends in a status the host reads instead of a
+// hung context.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+constexpr unsigned kWaitMaxSpins = 1u << 26;
+
+// Returns false (and flags ST_TIMEOUT) if the phase did not complete within the limit.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* status) {
-  for (unsigned it = 0; it < (1u << 24); ++it) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (unsigned it = 0; it < kWaitMaxSpins; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63u) == 63u && globaltimer_ns() - t0 > kWaitLimitNs) break;
     if (it > 64) __nanosleep(32);
   }
   atomicOr(status, ST_TIMEOUT);

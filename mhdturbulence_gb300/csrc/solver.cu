@@ -94,6 +94,18 @@ __global__ void k_ctrl_restore(Ctrl* c, unsigned long long step, double time, do
 // Point the step's host copy of U at v (null: none), in the launch descriptor on the device.
 __global__ void k_set_host_u(InstanceDesc* d, double* v) { d->a.Uh = v; }
 
+// Failure-detection self-test: one thread waits on an mbarrier that no arrival or copy ever
+// completes.  The bounded wait (the one the fused step uses for its plane loads) gives up, sets
+// ST_TIMEOUT in *status, and the kernel returns normally.
+__global__ void k_wait_selftest(unsigned* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_wait(&bar, 0u, status);
+  }
+}
+
 __global__ void k_ctrl_set_stop(Ctrl* c, double tmax, unsigned long long max_step) {
   c->tmax = tmax;
   c->max_step = max_step;
@@ -1175,6 +1187,35 @@ int mhdgb_selftest_division(int device, int n, unsigned long long seed, double* 
   cudaFree(d);
   if (e != cudaSuccess) return MHDGB_ERR_CUDA;
   *max_ulp = (double)h;
+  return MHDGB_OK;
+}
+
+int mhdgb_selftest_wait_timeout(int device, double* seconds, unsigned* status) {
+  if (!seconds || !status) return MHDGB_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MHDGB_ERR_CUDA;
+  unsigned* d = nullptr;
+  if (cudaMalloc(&d, sizeof(*d)) != cudaSuccess) return MHDGB_ERR_NOMEM;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMemset(d, 0, sizeof(*d));
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaEventRecord(e0);
+  if (e == cudaSuccess) {
+    k_wait_selftest<<<1, 32>>>(d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  unsigned h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d);
+  if (e != cudaSuccess) return MHDGB_ERR_CUDA;
+  *seconds = ms * 1e-3;
+  *status = h;
   return MHDGB_OK;
 }
 
