@@ -348,6 +348,15 @@ def run_ours(args, ws, rank, local):
                           "traffic": (prof_m["dram_bytes_per_cell"] * cells) if prof_m and
                           prof_m.get("dram_bytes_per_cell") else None},
              "clocks": mx["clocks"]}
+    if prof_m and prof_m.get("warp_inst_per_cell") and mx["clocks"].get("sm_mhz"):
+        # the mixed step's bound is instruction issue: the warp instructions per cell (ncu) against
+        # one warp instruction per clock per SM sub-partition (4 per SM) at the sampled SM clock
+        import torch
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        peak = nsm * 4 * mx["clocks"]["sm_mhz"] * 1e6
+        ach = prof_m["warp_inst_per_cell"] * (mx_value / ws) * 1e9
+        mixed["issue"] = {"achieved": ach / 1e9, "peak": peak / 1e9, "unit": "G warp-instructions/s",
+                          "frac": ach / peak, "warp_inst_per_cell": prof_m["warp_inst_per_cell"]}
     if not args.no_error:
         mixed["error_vs_fp64"] = mixed_error(n, args.error_steps, local)
     cpu = None
