@@ -182,7 +182,8 @@ def run_reference(args, ws, rank):
     rate, threads, steps, el = cpu_oracle_rate(args.n, args.cpu_seconds_ref, warm=max(1, min(args.warmup, 2)),
                                                max_steps=args.steps)
     sample = (f"KH {args.n}^3 FP64, {steps} full steps after warm-up, {el:.1f} s wall, OMP threads={threads} "
-              "(oracle port of src_cpp_kokkos_host; the reference tree is not on this host)")
+              "(oracle port of src_cpp_kokkos_host: the reference's own build needs Kokkos and MPI, which "
+              "this host lacks, and its sources do not travel to the GPU host)")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "Gcell-updates/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
