@@ -12,7 +12,8 @@ of mhdturbulence_gb300/ic.py, generated on the device by mhdgb_init_kh).
 Prints one JSON line.  value = whole-job Gcell-updates/s of the FP64 form with the state resident
 in HBM (CUDA events on the launching stream, W warm-up steps, then K timed steps; the 150^3 state
 is ~1 GB, larger than L2, so no flush is needed); e2e = the same through mhdgb_step_host with the
-state in pinned host memory copied in and out every step; "mixed" = the FP32-mixed form on the same
+state in pinned host memory, moved in and out every step (298 MB each way over the host link);
+"mixed" = the FP32-mixed form on the same
 configuration with its error against the FP64 form; cpu_baseline = the oracle (the reference's
 arithmetic restated in C, OpenMP) on this host's cores.
 
