@@ -112,17 +112,23 @@ __device__ __forceinline__ R fsqrt(R x) {
 }
 
 // sqrt of quantities that only estimate wave speeds (sound and fast speeds, the dt and c_h
-// candidates): in the FP64 fast build one Goldschmidt iteration without the final correction
-// (relative error ~2^-44, four FP64 operations); sqrt otherwise.
+// candidates).  FP64 fast build: the FP32 root g0 = x y (y the MUFU reciprocal square root of the
+// narrowed x, error ~2^-22) and one Newton correction g0 + (x - g0^2) y / 2, whose residual is
+// formed exactly by an FP64 FMA and scaled in FP32 (relative error ~2^-43, two FP64 operations).
+// Arguments outside [2^-80, 2^100] (below it a residual that still matters, down to 2x * 2^-43,
+// could underflow FP32), zero, negatives, inf and NaN take the IEEE square root.  sqrt otherwise.
 template <class R>
 __device__ __forceinline__ R fsqrt_est(R x) {
   if constexpr (kFast && std::is_same<R, double>::value) {
-    if (!sqrt_seed_range(x)) return sqrt(x);
+    const unsigned e = (unsigned)__double2hiint(x) >> 20;  // the sign bit makes negatives fail
+    if (e - (1023u - 80u) > 180u) return sqrt(x);
+    const float xf = d2f_rne(x);
     float yf;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(d2f_rne(x)));
-    const double y = f2d_exact(yf);
-    const double g = x * y;
-    return fma(g, fma(-g, 0.5 * y, 0.5), g);
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
+    const float g0 = xf * yf;
+    const double g0d = f2d_exact(g0);
+    const double d = fma(-g0d, g0d, x);
+    return g0d + f2d_exact(d2f_rne(d) * (0.5f * yf));
   } else {
     return sqrt(x);
   }
