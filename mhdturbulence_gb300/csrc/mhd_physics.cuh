@@ -62,13 +62,26 @@ __device__ __forceinline__ bool abs_less(float x, float lim) { return fabsf(x) <
 __device__ __forceinline__ float imin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float imax(float a, float b) { return (a < b) ? b : a; }
 
+// Narrowing and widening for FP32 seeds only.  The callers have checked that the argument is a
+// finite normal number well inside the float range, and a seed needs no rounding (the Newton steps
+// that follow remove its error), so the narrowing truncates the mantissa (error < 2^-23) and the
+// widening skips the zero and denormal cases: a few integer operations each, off the FP64 pipe.
+__device__ __forceinline__ float seed_narrow(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  return __uint_as_float((hi & 0x80000000u) | (((hi & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ double seed_widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  return __hiloint2double((int)((u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + (896u << 20))), (int)(u << 29));
+}
+
 // FP64 reciprocal from an FP32 seed (integer-pipe narrowing, the MUFU approximate reciprocal) and two
 // Newton-Raphson steps r <- r + r(1 - b r): the error of the seed (~2^-22) squares at each step,
 // so the result is within about one ulp of 1/b.
 __device__ __forceinline__ double rcp_newton(double b) {
   float sf;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(d2f_rne(b)));
-  double r = f2d_exact(sf);
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(seed_narrow(b)));
+  double r = seed_widen(sf);
   r = fma(r, fma(-b, r, 1.0), r);
   r = fma(r, fma(-b, r, 1.0), r);
   return r;
@@ -86,8 +99,8 @@ __device__ __forceinline__ bool sqrt_seed_range(double x) {
 }
 __device__ __forceinline__ double sqrt_goldschmidt(double x, double* inv = nullptr) {
   float yf;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(d2f_rne(x)));
-  const double y = f2d_exact(yf);
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(seed_narrow(x)));
+  const double y = seed_widen(yf);
   double g = x * y, h = 0.5 * y;
   const double r = fma(-g, h, 0.5);
   g = fma(g, r, g);
@@ -122,11 +135,11 @@ __device__ __forceinline__ R fsqrt_est(R x) {
   if constexpr (kFast && std::is_same<R, double>::value) {
     const unsigned e = (unsigned)__double2hiint(x) >> 20;  // the sign bit makes negatives fail
     if (e - (1023u - 80u) > 180u) return sqrt(x);
-    const float xf = d2f_rne(x);
+    const float xf = seed_narrow(x);
     float yf;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
     const float g0 = xf * yf;
-    const double g0d = f2d_exact(g0);
+    const double g0d = seed_widen(g0);
     const double d = fma(-g0d, g0d, x);
     return g0d + f2d_exact(d2f_rne(d) * (0.5f * yf));
   } else {
@@ -157,8 +170,8 @@ __device__ __forceinline__ R fdiv_est(R a, R b) {
     const unsigned e = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
     if (e < 1023u - 120u || e > 1023u + 120u) return a / b;
     float sf;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(d2f_rne(b)));
-    const double r = f2d_exact(sf);
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(seed_narrow(b)));
+    const double r = seed_widen(sf);
     return a * fma(r, fma(-b, r, 1.0), r);
   } else {
     return fdiv(a, b);
@@ -172,8 +185,8 @@ __device__ __forceinline__ double twice_div_est(double p, double s) {
   const unsigned e = ((unsigned)__double2hiint(s) >> 20) & 0x7FFu;
   if (e < 1023u - 120u || e > 1023u + 120u) return (p + p) / s;
   float r0;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d2f_rne(s)));
-  const double h = f2d_exact(r0), y0 = f2d_exact(2.0f * r0);
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(seed_narrow(s)));
+  const double h = seed_widen(r0), y0 = seed_widen(2.0f * r0);
   return p * fma(h, fma(-s, y0, 2.0), y0);
 }
 
