@@ -22,7 +22,7 @@ be built on this machine (they need Kokkos and MPI, and the reference tree is ab
 oracle port stands in for it, with all host threads.
 
 Multi-GPU (torchrun): every rank advances its own independent 150^3 replica ("replicas only": the
-path has no exchange in this build), timings are max-reduced over ranks, value sums all ranks.
+path has no exchange here), timings are max-reduced over ranks, value sums all ranks.
 """
 from __future__ import annotations
 

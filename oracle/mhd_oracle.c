@@ -2,8 +2,8 @@
  * mhd_oracle.c -- CPU restatement of the MHDTurbulence FP64 solver step.
  *
  * TEST INFRASTRUCTURE ONLY (the oracle).  Nothing in the shipped library links or calls this
- * file; tests/, __graft_entry__.smoke() and bench.py's CPU legs use it as the checker and as the
- * timed CPU baseline ("port").
+ * file; tests/, __graft_entry__.smoke() and bench.py's CPU legs use it as the reference for
+ * comparisons and as the timed CPU baseline ("port").
  *
  * Every function restates one stage of the reference's src_cpp_kokkos_host path with the same
  * floating-point operation order (left-to-right evaluation as in the C++ source), so that built

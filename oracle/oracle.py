@@ -1,7 +1,7 @@
 """ctypes binding of the oracle (oracle/mhd_oracle.c).  TEST INFRASTRUCTURE ONLY.
 
-Used by tests/ as the checker, by __graft_entry__.smoke() as the checker and by bench.py's CPU
-legs as the timed CPU baseline.  The shipped library never imports this module.
+Used by tests/ and __graft_entry__.smoke() as the reference the GPU results are compared with,
+and by bench.py's CPU legs as the timed CPU baseline.  The shipped library never imports this module.
 Arrays are numpy float64 in the reference FieldArray layout, shape (ktot, jtot, nv, itot).
 """
 from __future__ import annotations
