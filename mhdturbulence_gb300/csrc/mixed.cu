@@ -5,6 +5,7 @@
 #define MHDGB_FAST 1
 #define MHDGB_VNS v_mixed
 #include "fused.cuh"
+#include "fused_fs.cuh"
 #include "kernels.h"
 
 namespace mhdgb {
@@ -18,6 +19,7 @@ int variants_mixed(const FusedVariant** out) {
       v_mixed::FusedLauncher<float, 64, 4, 256>::variant(FUSED_MIXED),
       v_mixed::FusedLauncher<float, 32, 4, 256, 2>::variant(FUSED_MIXED),
       v_mixed::FusedLauncher<float, 16, 8, 256, 2>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncherFS<16, 8, 256, 2>::variant(FUSED_MIXED),
       // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
       v_mixed::FusedLauncher<float, 32, 4, 256, 2, true>::variant(FUSED_MIXED),
   };
