@@ -21,7 +21,7 @@ int variants_mixed(const FusedVariant** out) {
       v_mixed::FusedLauncher<float, 16, 8, 256, 2>::variant(FUSED_MIXED),
       v_mixed::FusedLauncherFS<16, 8, 256, 2>::variant(FUSED_MIXED),
       // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
-      v_mixed::FusedLauncher<float, 32, 4, 256, 2, true>::variant(FUSED_MIXED),
+      v_mixed::FusedLauncherFS<16, 8, 256, 2, true>::variant(FUSED_MIXED),
   };
   *out = v;
   return (int)(sizeof(v) / sizeof(v[0])) - 1;  // the last entry is the run-time solver kernel
