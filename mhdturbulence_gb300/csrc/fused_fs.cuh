@@ -161,6 +161,11 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
     const FastDiv dv0(cx), dv1(cx + 1);
 
     for (int k = kb; k < ke; k++) {
+      if (own) {  // the cell's U is read after the faces of this plane: pull it into L2 now
+        const double* u0 = a.U + L.at(NCONS, 0, k + NGH, jj + NGH, ii + NGH);
+#pragma unroll
+        for (int m = 0; m < NCONS; m++) prefetch_l2(u0 + m * fsU);
+      }
       if (k > kb) wait_plane(k + 2);
       const int fb = k & 1;
       // ---- faces of plane k (on the first plane also the faces kb-1/2, into LOW) ----
