@@ -229,9 +229,9 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
 #pragma unroll
           for (int n = 0; n < NPRIM; n++) {
             const int v = var_of(n) * PX;
-            const R s0 = c0[v], s1 = c1[v], s2 = c2[v], s3 = c3[v];
-            pl[n] = left_state(s1, van_leer(s2 - s1, s1 - s0));   // slope of the left cell
-            pr[n] = right_state(s2, van_leer(s3 - s2, s2 - s1));  // slope of the right cell
+            const float2 st = van_leer_states_pair(c0[v], c1[v], c2[v], c3[v]);  // both cells' slopes
+            pl[n] = st.x;
+            pr[n] = st.y;
           }
           face_flux<R, 0>(pl, pr, glm, f, riemann, rot);
           auto slot_of_flux = [&](int m) {

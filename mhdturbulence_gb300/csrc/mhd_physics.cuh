@@ -62,6 +62,13 @@ __device__ __forceinline__ bool abs_less(float x, float lim) { return fabsf(x) <
 __device__ __forceinline__ float imin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float imax(float a, float b) { return (a < b) ? b : a; }
 
+// The MUFU approximate reciprocal of an FP32 value (flushes denormals).
+__device__ __forceinline__ float rcp_approx_f32(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Narrowing and widening for FP32 seeds only.  The callers have checked that the argument is a
 // finite normal number well inside the float range, and a seed needs no rounding (the Newton steps
 // that follow remove its error), so the narrowing truncates the mantissa (error < 2^-23) and the
@@ -200,12 +207,28 @@ __device__ __forceinline__ R van_leer(R dsvp, R dsvm) {
     const R p = dsvp * dsvm;
     if constexpr (std::is_same<R, double>::value) {
       return pos_nonzero(p) ? twice_div_est(p, dsvp + dsvm) : R(0);
-    } else {
-      return (p > R(0)) ? fdiv_est(p + p, dsvp + dsvm) : R(0);
+    } else {  // FP32: (p + p) times the MUFU reciprocal, the form the paired evaluation repeats
+      return (p > R(0)) ? (p + p) * rcp_approx_f32(dsvp + dsvm) : R(0);
     }
   } else {
     return (dsvp * dsvm > R(0)) ? fdiv(R(2) * dsvp * dsvm, dsvp + dsvm) : R(0);
   }
+}
+
+// The slopes of two adjacent cells at once, from the stencil s0 s1 s2 s3 of a face: the left
+// cell's van_leer(s2-s1, s1-s0) and the right cell's van_leer(s3-s2, s2-s1), with packed FP32
+// instructions (two lanes per instruction); each lane rounds as the scalar van_leer<float> does,
+// so the results are the same bit for bit.  Returns the face's states (s1 + sl/2, s2 - sr/2).
+__device__ __forceinline__ float2 van_leer_states_pair(float s0, float s1, float s2, float s3) {
+  const float2 lo = make_float2(s0, s1), mid = make_float2(s1, s2);
+  const float2 dm = __ffma2_rn(lo, make_float2(-1.0f, -1.0f), mid);  // (s1 - s0, s2 - s1), exact as a subtraction
+  const float2 dp = make_float2(dm.y, s3 - s2);                      // (s2 - s1, s3 - s2)
+  const float2 p = __fmul2_rn(dp, dm);
+  const float2 sum = __fadd2_rn(dp, dm);
+  const float2 pp = __fadd2_rn(p, p);
+  const float2 q = __fmul2_rn(pp, make_float2(rcp_approx_f32(sum.x), rcp_approx_f32(sum.y)));
+  const float2 sl = make_float2(p.x > 0.0f ? q.x : 0.0f, p.y > 0.0f ? q.y : 0.0f);
+  return __ffma2_rn(sl, make_float2(0.5f, -0.5f), mid);
 }
 
 // Rotation maps of Prim2Cons1/2/3, mhd.cpp:1078-1118.
