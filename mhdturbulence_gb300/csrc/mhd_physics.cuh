@@ -154,14 +154,18 @@ __device__ __forceinline__ R fsqrt_est(R x) {
   }
 }
 
-// a / b: IEEE division in the exact build and in FP32; a * rcp_newton(b) in the FP64 fast build
-// (within ~1.5 ulp), with IEEE division where |b| is outside the FP32 seed's range.
+// a / b: IEEE division in the exact build; a * rcp_newton(b) in the FP64 fast build (within ~1.5
+// ulp), with IEEE division where |b| is outside the FP32 seed's range; in the FP32 (mixed) build a
+// times the MUFU reciprocal (within ~2 ulp, like the build's approximate division, with fewer
+// instructions).
 template <class R>
 __device__ __forceinline__ R fdiv(R a, R b) {
   if constexpr (kFast && std::is_same<R, double>::value) {
     const unsigned e = ((unsigned)__double2hiint(b) >> 20) & 0x7FFu;
     if (e < 1023u - 120u || e > 1023u + 120u) return a / b;
     return a * rcp_newton(b);
+  } else if constexpr (kFast && std::is_same<R, float>::value) {
+    return a * rcp_approx_f32(b);
   } else {
     return a / b;
   }
