@@ -349,6 +349,42 @@ __device__ __forceinline__ void prim2cons_state(const R (&Prim)[NPRIM], R (&Cons
   Cons[mvel] = Prim[D::nved];
   Cons[mpre] = Prim[npre] + bsq / R(2);
 }
+// prim2cons_state of a face's two states at once (FP32, rotated frame as Dir<0>): P[n] holds the
+// left and right primitive, C[q] receives the two state vectors, with packed FP32 instructions (two
+// lanes per instruction) and a fixed order of operations; the sums over the components keep the
+// unrotated x, y, z order as sum_sq3 does.
+__device__ __forceinline__ void prim2cons_state_pair(const float2 (&P)[NPRIM], float2 (&C)[NVEC], int rot) {
+  const float2 half = make_float2(0.5f, 0.5f);
+  auto sq3 = [&](int b) {  // P[b]^2 + P[b+1]^2 + P[b+2]^2 in the unrotated order
+    const float2 r0 = P[b], r1 = P[b + 1], r2 = P[b + 2];
+    const float2 x = rot == 0 ? r0 : (rot == 1 ? r2 : r1);
+    const float2 y = rot == 0 ? r1 : (rot == 1 ? r0 : r2);
+    const float2 z = rot == 0 ? r2 : (rot == 1 ? r1 : r0);
+    return __ffma2_rn(z, z, __ffma2_rn(y, y, __fmul2_rn(x, x)));
+  };
+  const float2 rho = P[nden];
+  const float2 rinv = make_float2(rcp_approx_f32(rho.x), rcp_approx_f32(rho.y));
+  const float2 vsq = sq3(nve1), bsq = sq3(nbm1);
+  C[mudn] = rho;
+  C[muvu] = __fmul2_rn(rho, P[nve1]);
+  C[muvv] = __fmul2_rn(rho, P[nve2]);
+  C[muvw] = __fmul2_rn(rho, P[nve3]);
+  C[muet] = __ffma2_rn(half, bsq, __ffma2_rn(__fmul2_rn(half, rho), vsq, __fmul2_rn(rho, P[nene])));
+  C[mubu] = P[nbm1];
+  C[mubv] = P[nbm2];
+  C[mubw] = P[nbm3];
+  C[mubp] = P[nbps];
+  C[must] = __fmul2_rn(rho, P[nst]);
+  const float2 css = __fmul2_rn(P[ncsp], P[ncsp]);
+  const float2 cts = __ffma2_rn(bsq, rinv, css);
+  const float2 ca = __fmul2_rn(__fmul2_rn(P[nbm1], P[nbm1]), rinv);  // normal-field Alfven speed squared
+  const float2 disc = __ffma2_rn(cts, cts, __fmul2_rn(make_float2(-4.0f, -4.0f), __fmul2_rn(css, ca)));
+  const float2 cf2 = __fmul2_rn(half, __fadd2_rn(cts, make_float2(sqrtf(disc.x), sqrtf(disc.y))));
+  C[mcsp] = make_float2(sqrtf(cf2.x), sqrtf(cf2.y));
+  C[mvel] = P[nve1];
+  C[mpre] = __ffma2_rn(half, bsq, P[npre]);
+}
+
 // The flux slots (mfdn .. mfst) of Cons from the primitive state and Cons[muet], Cons[mpre].
 template <class R, int DIR>
 __device__ __forceinline__ void prim2cons_flux(const R (&Prim)[NPRIM], R (&Cons)[NVEC], int rot = 0) {
@@ -768,8 +804,21 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
   constexpr bool branch_hlld = kFast;
   if (branch_hlld && riemann == RIEMANN_HLLD) {  // the upwind flux is formed inside hlld_branch
-    prim2cons_state<R, DIR>(Pl, Cl, rot);
-    prim2cons_state<R, DIR>(Pr, Cr, rot);
+    if constexpr (std::is_same<R, float>::value && DIR == 0) {  // FP32: both sides in packed pairs
+      float2 P2[NPRIM], C2[NVEC];
+#pragma unroll
+      for (int n = 0; n < NPRIM; n++) P2[n] = make_float2(Pl[n], Pr[n]);
+      prim2cons_state_pair(P2, C2, rot);
+      constexpr int set[] = {mudn, muvu, muvv, muvw, muet, mubu, mubv, mubw, mubp, must, mcsp, mvel, mpre};
+#pragma unroll
+      for (int t = 0; t < (int)(sizeof(set) / sizeof(set[0])); t++) {
+        Cl[set[t]] = C2[set[t]].x;
+        Cr[set[t]] = C2[set[t]].y;
+      }
+    } else {
+      prim2cons_state<R, DIR>(Pl, Cl, rot);
+      prim2cons_state<R, DIR>(Pr, Cr, rot);
+    }
   } else {
     prim2cons<R, DIR>(Pl, Cl, rot);
     prim2cons<R, DIR>(Pr, Cr, rot);
