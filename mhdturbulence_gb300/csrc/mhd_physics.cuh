@@ -349,6 +349,16 @@ __device__ __forceinline__ void prim2cons_state(const R (&Prim)[NPRIM], R (&Cons
   Cons[mvel] = Prim[D::nved];
   Cons[mpre] = Prim[npre] + bsq / R(2);
 }
+// The left (x) and right (y) lanes of packed state pairs, indexed like a state vector.
+struct PairLo {
+  const float2* c;
+  __device__ __forceinline__ float operator[](int q) const { return c[q].x; }
+};
+struct PairHi {
+  const float2* c;
+  __device__ __forceinline__ float operator[](int q) const { return c[q].y; }
+};
+
 // prim2cons_state of a face's two states at once (FP32, rotated frame as Dir<0>): P[n] holds the
 // left and right primitive, C[q] receives the two state vectors, with packed FP32 instructions (two
 // lanes per instruction) and a fixed order of operations; the sums over the components keep the
@@ -560,8 +570,9 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
 // forms are taken only when their conditions hold, and only the upwind side's physical flux is
 // formed (face_flux() passes states without flux slots; prim2cons_flux() fills the upwind side's).
 // Results agree with hlld() to rounding (and in the sign of zero results).
-template <class R, int DIR>
-__device__ __forceinline__ void hlld_branch(const R (&leftst)[NVEC], const R (&rigtst)[NVEC], const R (&Pl)[NPRIM],
+// leftst / rigtst: the two state vectors, as arrays or as PairLo / PairHi views of packed pairs.
+template <class R, int DIR, class CL, class CR>
+__device__ __forceinline__ void hlld_branch(const CL& leftst, const CR& rigtst, const R (&Pl)[NPRIM],
                                             const R (&Pr)[NPRIM], R (&nflux)[NCONS], int rot = 0) {
   using D = Dir<DIR>;
   const R eps = R(1.0e-30);
@@ -803,22 +814,30 @@ __device__ __forceinline__ void face_flux(const R (&Pl)[NPRIM], const R (&Pr)[NP
   using D = Dir<DIR>;
   R Cl[NVEC], Cr[NVEC], nf[NCONS];
   constexpr bool branch_hlld = kFast;
-  if (branch_hlld && riemann == RIEMANN_HLLD) {  // the upwind flux is formed inside hlld_branch
-    if constexpr (std::is_same<R, float>::value && DIR == 0) {  // FP32: both sides in packed pairs
+  if constexpr (branch_hlld && std::is_same<R, float>::value && DIR == 0) {
+    if (riemann == RIEMANN_HLLD) {  // FP32: both sides' states in packed pairs, read in place by HLLD
       float2 P2[NPRIM], C2[NVEC];
 #pragma unroll
       for (int n = 0; n < NPRIM; n++) P2[n] = make_float2(Pl[n], Pr[n]);
       prim2cons_state_pair(P2, C2, rot);
-      constexpr int set[] = {mudn, muvu, muvv, muvw, muet, mubu, mubv, mubw, mubp, must, mcsp, mvel, mpre};
-#pragma unroll
-      for (int t = 0; t < (int)(sizeof(set) / sizeof(set[0])); t++) {
-        Cl[set[t]] = C2[set[t]].x;
-        Cr[set[t]] = C2[set[t]].y;
-      }
-    } else {
-      prim2cons_state<R, DIR>(Pl, Cl, rot);
-      prim2cons_state<R, DIR>(Pr, Cr, rot);
+      hlld_branch<R, DIR>(PairLo{C2}, PairHi{C2}, Pl, Pr, nf, rot);
+      F[mden] = nf[mden];
+      F[mrv1] = nf[D::orv1];
+      F[mrv2] = nf[D::orv2];
+      F[mrv3] = nf[D::orv3];
+      F[meto] = nf[meto];
+      F[D::ob_a] = nf[D::sb_a];
+      F[D::ob_b] = nf[D::sb_b];
+      const R bpl = C2[mubp].x, bpr = C2[mubp].y, bul = C2[mubu].x, bur = C2[mubu].y;
+      F[D::glm] = R(0.5) * (bpl + bpr) - R(0.5) * chg * (bur - bul);
+      F[mbps] = (R(0.5) * (bul + bur) - fdiv(R(0.5), chg) * (bpr - bpl)) * chg * chg;
+      F[mst] = nf[mst];
+      return;
     }
+  }
+  if (branch_hlld && riemann == RIEMANN_HLLD) {  // the upwind flux is formed inside hlld_branch
+    prim2cons_state<R, DIR>(Pl, Cl, rot);
+    prim2cons_state<R, DIR>(Pr, Cr, rot);
   } else {
     prim2cons<R, DIR>(Pl, Cl, rot);
     prim2cons<R, DIR>(Pr, Cr, rot);
