@@ -50,6 +50,8 @@ cudaError_t fdiv_selftest(int n, unsigned long long seed, unsigned long long* d_
   return cudaGetLastError();
 }
 
+int preferred_fp64() { return 4; }  // 16x8 cells, 256 threads
+
 int variants_fp64(const FusedVariant** out) {
   static const FusedVariant v[] = {
       v_fast64::FusedLauncher<double, 32, 4, 128>::variant(FUSED_FP64),

@@ -11,6 +11,8 @@
 namespace mhdgb {
 namespace detail {
 
+int preferred_mixed() { return 6; }  // the fused-slope kernel, 16x8 cells, two CTAs per SM
+
 int variants_mixed(const FusedVariant** out) {
   static const FusedVariant v[] = {
       v_mixed::FusedLauncher<float, 32, 4, 128>::variant(FUSED_MIXED),

@@ -644,12 +644,13 @@ int create_impl(const mhdgb_config* cfg, cudaStream_t shared, mhdgb_solver** out
   h->x3a = face_axis(cfg->nz, cfg->x3min, cfg->x3max);
   if ((rc = upload_grid(h))) return cleanup(rc);
   {
-    int idx = 0;
+    int idx = fused_preferred_variant(h->kind);
+    if (idx >= h->nvars) idx = 0;
     std::lock_guard<std::mutex> g(g_tune_mu);
     auto& m = tune_cache();
     auto it = m.find(std::make_tuple((int)h->kind, L.nx, L.ny, L.nz));
     if (it != m.end() && it->second < h->nvars) idx = it->second;
-    if ((rc = use_variant(h, idx, 4))) return cleanup(rc);
+    if ((rc = use_variant(h, idx, 4)) && (idx == 0 || (rc = use_variant(h, 0, 4)))) return cleanup(rc);
   }
   k_ctrl_reset<<<1, 1, 0, h->stream>>>(h->ctrl, 0);
   k_ctrl_set_stop<<<1, 1, 0, h->stream>>>(h->ctrl, 1.0e300, ~0ull);
@@ -1472,7 +1473,9 @@ int mhdgb_ensemble_create(int n, const mhdgb_config* cfgs, mhdgb_ensemble** out)
     mhdgb_ensemble_destroy(e);
     return MHDGB_ERR_NOMEM;
   }
-  int rc = ens_use_variant(e, 0);
+  const int pref = fused_preferred_variant(e->kind);
+  int rc = ens_use_variant(e, pref < e->nvars ? pref : 0);
+  if (rc && pref != 0) rc = ens_use_variant(e, 0);
   if (rc) { mhdgb_ensemble_destroy(e); return rc; }
   *out = e;
   return MHDGB_OK;

@@ -361,6 +361,14 @@ cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm,
 }
 }  // namespace detail
 
+int fused_preferred_variant(FusedKind kind) {
+  switch (kind) {
+    case FUSED_FP64_EXACT: return 0;
+    case FUSED_FP64: return detail::preferred_fp64();
+    default: return detail::preferred_mixed();
+  }
+}
+
 int fused_variants(FusedKind kind, const FusedVariant** out) {
   switch (kind) {
     case FUSED_FP64_EXACT: return detail::variants_exact(out);

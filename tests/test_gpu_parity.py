@@ -262,6 +262,12 @@ def test_every_tile_shape_gives_identical_results(precision):
             assert rel_linf(ic.interior(o), ic.interior(outs[0])) <= 1e-9
         else:
             assert np.array_equal(o, outs[0])
+    if precision == "mixed":  # bit for bit within each register build: at most two distinct results
+        classes = []
+        for o in outs:
+            if not any(np.array_equal(o, c) for c in classes):
+                classes.append(o)
+        assert len(classes) <= 2, len(classes)
 
 
 def test_autotune_restores_state_and_is_remembered():
