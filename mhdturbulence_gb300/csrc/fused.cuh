@@ -259,6 +259,52 @@ __device__ __forceinline__ void update_cell(const DivAcc<float>& acc, const doub
   u[mbps] = u[mbps] * f2d_exact(1.0f - dtf * (0.1f * chf * imax));
 }
 
+// Launch-wide steps shared by the fused-step kernels.
+// Start of a launch: block 0 resets every live grid's reduction slot (step+2)%3 for the next launch
+// (step n reduces into slot (n+1)%3).
+__device__ __forceinline__ void fused_reset_next_slots(const InstanceDesc* __restrict__ desc, int ninst, int nt) {
+  if (blockIdx.x != 0) return;
+  for (int q = threadIdx.x; q < ninst; q += nt) {
+    Ctrl* c = desc[q].a.ctrl;
+    if (!c->done) {
+      c->slot[(c->step + 2) % 3].dtmin_bits = DT_RESET;
+      c->slot[(c->step + 2) % 3].chmax_bits = CH_RESET;
+    }
+  }
+}
+// The grid a queue item belongs to (the descriptors are sorted by item_begin).
+__device__ __forceinline__ int fused_instance_of(const InstanceDesc* __restrict__ desc, int ninst, int gitem) {
+  int inst = 0;
+  for (int lo = 0, hi = ninst - 1; lo <= hi;) {
+    const int mid = (lo + hi) >> 1;
+    if (desc[mid].item_begin <= gitem) { inst = mid; lo = mid + 1; } else hi = mid - 1;
+  }
+  return inst;
+}
+// End of a CTA (thread 0): the last CTA to finish advances every live grid by one step and re-arms
+// the work queue for the next launch.
+__device__ __forceinline__ void fused_finish_cta(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc,
+                                                 int ninst) {
+  __threadfence();
+  const unsigned prev = atomicAdd(&lc->blocks_done, 1u);
+  if (prev == gridDim.x - 1) {
+    __threadfence();
+    for (int q = 0; q < ninst; q++) {
+      Ctrl* c = desc[q].a.ctrl;
+      if (c->done) continue;
+      const double dtq = desc[q].a.cfl * bitsd(c->slot[c->step % 3].dtmin_bits);
+      c->last_dt = dtq;
+      c->last_ch = bitsd(c->slot[c->step % 3].chmax_bits);
+      c->time += dtq;
+      c->step += 1;
+      if (c->time > c->tmax || c->step >= c->max_step) c->done = 1;
+    }
+    lc->work_next = 0;
+    lc->blocks_done = 0;
+    __threadfence();
+  }
+}
+
 // MINB: CTAs per SM the register allocation must allow (__launch_bounds__); 2 at 256 threads caps
 // a thread at 128 registers, which the FP32 form meets without spills.
 // GEN: false compiles HLLD alone (the tuned tile variants); true reads the Riemann solver from the
@@ -286,15 +332,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
 
   const int tid = threadIdx.x;
   const int ninst = (int)lc->ninst, total = (int)lc->total_items;
-  // step n of a grid reduces into slot (n+1)%3; slot (n+2)%3 is reset here for the next launch
-  if (blockIdx.x == 0)
-    for (int q = tid; q < ninst; q += NT) {
-      Ctrl* c = desc[q].a.ctrl;
-      if (!c->done) {
-        c->slot[(c->step + 2) % 3].dtmin_bits = DT_RESET;
-        c->slot[(c->step + 2) % 3].chmax_bits = CH_RESET;
-      }
-    }
+  fused_reset_next_slots(desc, ninst, NT);
   if (tid == 0) {
     for (int s = 0; s < NBUF; s++) mbar_init(&bars[s], 1);
     fence_mbar_init();
@@ -313,11 +351,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     __syncthreads();
     const int gitem = s_item;
     if (gitem >= total || s_abort) break;
-    int inst = 0;  // the grid this work item belongs to
-    for (int lo = 0, hi = ninst - 1; lo <= hi;) {
-      const int mid = (lo + hi) >> 1;
-      if (desc[mid].item_begin <= gitem) { inst = mid; lo = mid + 1; } else hi = mid - 1;
-    }
+    const int inst = fused_instance_of(desc, ninst, gitem);  // the grid this work item belongs to
     const FusedArgs& a = desc[inst].a;
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) { __syncthreads(); continue; }
@@ -600,26 +634,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     for (int s = 0; s < NBUF; s++)
       if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &desc[0].a.ctrl->status);
   }
-  if (tid == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(&lc->blocks_done, 1u);
-    if (prev == gridDim.x - 1) {  // last CTA: advance every live grid by one step
-      __threadfence();
-      for (int q = 0; q < ninst; q++) {
-        Ctrl* c = desc[q].a.ctrl;
-        if (c->done) continue;
-        const double dtq = desc[q].a.cfl * bitsd(c->slot[c->step % 3].dtmin_bits);
-        c->last_dt = dtq;
-        c->last_ch = bitsd(c->slot[c->step % 3].chmax_bits);
-        c->time += dtq;
-        c->step += 1;
-        if (c->time > c->tmax || c->step >= c->max_step) c->done = 1;
-      }
-      lc->work_next = 0;
-      lc->blocks_done = 0;
-      __threadfence();
-    }
-  }
+  if (tid == 0) fused_finish_cta(desc, lc, ninst);
 }
 
 // Recovery of P from U for the interior (+ ghost images) and the dt/c_h reduction into slot: the

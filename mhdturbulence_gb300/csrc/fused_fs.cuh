@@ -63,15 +63,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
 
   const int tid = threadIdx.x;
   const int ninst = (int)lc->ninst, total = (int)lc->total_items;
-  // step n of a grid reduces into slot (n+1)%3; slot (n+2)%3 is reset here for the next launch
-  if (blockIdx.x == 0)
-    for (int q = tid; q < ninst; q += NT) {
-      Ctrl* c = desc[q].a.ctrl;
-      if (!c->done) {
-        c->slot[(c->step + 2) % 3].dtmin_bits = DT_RESET;
-        c->slot[(c->step + 2) % 3].chmax_bits = CH_RESET;
-      }
-    }
+  fused_reset_next_slots(desc, ninst, NT);
   if (tid == 0) {
     for (int s = 0; s < NBUF; s++) mbar_init(&bars[s], 1);
     fence_mbar_init();
@@ -89,11 +81,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
     __syncthreads();
     const int gitem = s_item;
     if (gitem >= total || s_abort) break;
-    int inst = 0;  // the grid this work item belongs to
-    for (int lo = 0, hi = ninst - 1; lo <= hi;) {
-      const int mid = (lo + hi) >> 1;
-      if (desc[mid].item_begin <= gitem) { inst = mid; lo = mid + 1; } else hi = mid - 1;
-    }
+    const int inst = fused_instance_of(desc, ninst, gitem);  // the grid this work item belongs to
     const FusedArgs& a = desc[inst].a;
     Ctrl* ctrl = a.ctrl;
     if (ctrl->done) { __syncthreads(); continue; }
@@ -307,26 +295,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
     for (int s = 0; s < NBUF; s++)
       if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &desc[0].a.ctrl->status);
   }
-  if (tid == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(&lc->blocks_done, 1u);
-    if (prev == gridDim.x - 1) {  // last CTA: advance every live grid by one step
-      __threadfence();
-      for (int q = 0; q < ninst; q++) {
-        Ctrl* c = desc[q].a.ctrl;
-        if (c->done) continue;
-        const double dtq = desc[q].a.cfl * bitsd(c->slot[c->step % 3].dtmin_bits);
-        c->last_dt = dtq;
-        c->last_ch = bitsd(c->slot[c->step % 3].chmax_bits);
-        c->time += dtq;
-        c->step += 1;
-        if (c->time > c->tmax || c->step >= c->max_step) c->done = 1;
-      }
-      lc->work_next = 0;
-      lc->blocks_done = 0;
-      __threadfence();
-    }
-  }
+  if (tid == 0) fused_finish_cta(desc, lc, ninst);
 }
 
 // Host side of one instantiation of k_fused_step_fs (the FusedLauncher interface).
