@@ -25,7 +25,8 @@
 // a CUDA graph.
 //
 // R is the arithmetic type of reconstruction, Riemann solve and the P buffers: double for the FP64
-// form, float for the mixed form.  The conserved state U and its update are FP64 in both forms; in
+// form, float for the mixed form (whose fastest variant, k_fused_step_fs in fused_fs.cuh, forms the
+// slopes inside the face phase instead).  The conserved state U and its update are FP64 in both forms; in
 // the mixed form the flux-divergence terms are summed with compensation (TwoProd/TwoSum in FP32) and
 // the pressure recovery e = (E - m^2/(2 rho) - B^2/2)/rho is FP64 (with 1/rho from an FP32 seed and
 // one FP64 Newton step).
