@@ -181,6 +181,10 @@ int mhdgb_time_steps(mhdgb_solver* h, int nsteps, double* ms);
 int mhdgb_variant_count(const mhdgb_solver* h);
 int mhdgb_variant_info(const mhdgb_solver* h, int idx, int* tx, int* ty, int* threads, int* current);
 int mhdgb_select_variant(mhdgb_solver* h, int idx);
+/* Kernel form and tile shape of variant idx, e.g. "two-phase 16x8/256" or "fused-slope 16x8/256 x2"
+ * (x2: compiled for two CTAs per SM); idx = -1 names the kernel in use, which for HLLE/HLLC is the
+ * run-time solver kernel.  NULL for an invalid index. */
+const char* mhdgb_variant_name(const mhdgb_solver* h, int idx);
 /* Time every compiled tile shape on the handle's grid (steps fused steps each, from the current
  * state, which is restored afterwards) and keep the fastest.  The choice is remembered per
  * (precision, nx, ny, nz) for later handles in the process and, if the environment variable
@@ -201,6 +205,14 @@ int mhdgb_selftest_division(int device, int n, unsigned long long seed, double* 
  * up after about 2 s and returns with the timeout bit (4) set in *status, leaving the context
  * usable.  *seconds receives the kernel's duration.  Nothing faults or hangs. */
 int mhdgb_selftest_wait_timeout(int device, double* seconds, unsigned* status);
+/* Self-test of the fused step's abort path (no reference counterpart): on a 32x24x16 KH grid of the
+ * given precision, one fused step runs with the first plane load of every work item expecting 16
+ * bytes more than the load delivers, so each CTA's bounded wait for that plane gives up after about
+ * 2 s, the CTA drains its other loads (bounded too) and returns.  *seconds is the step's duration and
+ * *status its device status bits (4 = wait timeout).  The same handle then runs two ordinary steps
+ * from a fresh state; *recovered = 1 if they report no error and equal those of a handle that never
+ * saw the aborted step, bit for bit.  Nothing faults or hangs. */
+int mhdgb_selftest_fused_abort(int device, int precision, double* seconds, unsigned* status, int* recovered);
 
 /* KH diagnostic of RealTimeAnalysis (src_cpp_kokkos_device/main.cpp:26-84):
  * out = {volume, <X(1-X)>, sqrt(<v_y^2>)} over the interior, FP64 sums. */
@@ -284,7 +296,9 @@ int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best);
  * of which a call uses 1536*(nx+ny+nz+7) bytes; calls with nx+ny+nz > MHDGB_NOALLOC_MAX_EXTENT_SUM
  * return MHDGB_ERR_SCRATCH before touching the device.  No part of the scratch has to start at zero.
  * The first call on each device resolves the scratch address (cudaGetSymbolAddress, which also loads
- * the module): make that first call before any stream capture begins.  All calls on one device share
+ * the module): make that first call before any stream capture begins.  A device reset
+ * (cudaDeviceReset) ends the context that address belongs to; the next call resolves it again, so
+ * after a reset, too, make one call before capturing.  All calls on one device share
  * the one scratch array, so calls that overlap in time -- on different streams, or from several host
  * threads without ordering between their streams -- race on it and give wrong ghosts; order them. */
 #define MHDGB_ERR_SCRATCH (-8) /* request larger than a fixed scratch area */

@@ -81,9 +81,11 @@ SIGNATURES = {
     "mhdgb_reset_clock": (C.c_int, [_vp]),
     "mhdgb_step_host": (C.c_int, [_vp, _dp, _dp, C.c_int, _dp, _dp]),
     "mhdgb_time_steps": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_selftest_fused_abort": (C.c_int, [C.c_int, C.c_int, _dp, C.POINTER(C.c_uint), C.POINTER(C.c_int)]),
     "mhdgb_variant_count": (C.c_int, [_vp]),
     "mhdgb_variant_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int)]),
+    "mhdgb_variant_name": (C.c_char_p, [_vp, C.c_int]),
     "mhdgb_select_variant": (C.c_int, [_vp, C.c_int]),
     "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mhdgb_measure_fp64_rate": (C.c_int, [C.c_int, _dp]),

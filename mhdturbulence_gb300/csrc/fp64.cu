@@ -50,15 +50,13 @@ cudaError_t fdiv_selftest(int n, unsigned long long seed, unsigned long long* d_
   return cudaGetLastError();
 }
 
-int preferred_fp64() { return 4; }  // 16x8 cells, 256 threads
-
 int variants_fp64(const FusedVariant** out) {
   static const FusedVariant v[] = {
       v_fast64::FusedLauncher<double, 32, 4, 128>::variant(FUSED_FP64),
       v_fast64::FusedLauncher<double, 28, 4, 128>::variant(FUSED_FP64),
       v_fast64::FusedLauncher<double, 16, 8, 128>::variant(FUSED_FP64),
       v_fast64::FusedLauncher<double, 32, 4, 256>::variant(FUSED_FP64),
-      v_fast64::FusedLauncher<double, 16, 8, 256>::variant(FUSED_FP64),
+      preferred_variant(v_fast64::FusedLauncher<double, 16, 8, 256>::variant(FUSED_FP64)),
       // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
       v_fast64::FusedLauncher<double, 16, 8, 256, 1, true>::variant(FUSED_FP64),
   };

@@ -32,6 +32,8 @@
 // one FP64 Newton step).
 #pragma once
 
+#include <cstdio>
+
 #include "common.cuh"
 #include "fused_args.h"
 #include "mhd_physics.cuh"
@@ -386,7 +388,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     auto plane = [&](int p) -> const R* { return ring + (size_t)slot_of(p) * S::PLANE; };
     auto issue = [&](int p) {  // thread 0 only
       const int s = slot_of(p);
-      mbar_arrive_expect_tx(&bars[s], S::plane_tx_bytes);
+      mbar_arrive_expect_tx(&bars[s], S::plane_tx_bytes + (p == kb - 2 ? a.tx_extra : 0u));
       tma_load_4d(ring + (size_t)s * S::PLANE, tmap, i0, 0, j0, p + NGH, &bars[s]);
     };
     auto wait_plane = [&](int p) {
@@ -711,8 +713,15 @@ struct FusedLauncher {
     k_fused_step<R, TX, TY, NT, MINB, GEN><<<grid, NT, S::total, s>>>(desc, lc);
     return cudaGetLastError();
   }
+  static const char* name() {
+    static char buf[64];
+    if (!buf[0])
+      std::snprintf(buf, sizeof(buf), "two-phase %dx%d/%d%s%s", TX, TY, NT, MINB > 1 ? " x2" : "",
+                    GEN ? " run-time solver" : "");
+    return buf;
+  }
   static FusedVariant variant(FusedKind kind) {
-    return FusedVariant{kind, shape(), &prepare, &ctas_per_sm, &launch};
+    return FusedVariant{kind, shape(), &prepare, &ctas_per_sm, &launch, name(), 0};
   }
 };
 

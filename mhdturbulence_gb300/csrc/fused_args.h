@@ -33,6 +33,10 @@ struct FusedArgs {
   // End-to-end steps: the caller's host array of U (reference layout, itot x jtot x ktot, reached
   // over the host link), written by the step's cell updates besides U; null otherwise.
   double* Uh;
+  // Bytes the first plane load of each work item is expected to deliver beyond the plane itself:
+  // 0 in every step; mhdgb_selftest_fused_abort sets it so that the wait for that plane runs out
+  // and the kernel's abort-and-drain path runs.
+  unsigned tx_extra;
 };
 
 // One grid of a launch: its arguments, the TMA maps of its two primitive buffers and its range of
@@ -59,6 +63,14 @@ struct FusedVariant {
   cudaError_t (*prepare)();    // set the kernel's shared-memory attribute on the current device
   int (*ctas_per_sm)();        // occupancy
   cudaError_t (*launch)(const InstanceDesc* desc, LaunchCtrl* lc, int grid, cudaStream_t s);
+  const char* name;            // kernel form and tile shape, e.g. "two-phase 16x8/256"
+  int preferred;               // 1: the entry a grid starts on before any autotuning
 };
+
+// Marks the table entry a grid starts on: the fastest measured on GB300 at the benchmark sizes.
+inline FusedVariant preferred_variant(FusedVariant v) {
+  v.preferred = 1;
+  return v;
+}
 
 }  // namespace mhdgb

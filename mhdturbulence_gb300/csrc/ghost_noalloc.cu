@@ -24,6 +24,8 @@
 //                    read from the snapshot where the reference's pack held an overwritten ghost and
 //                    from P's interior cells otherwise.  It reads no cell it writes.
 // The result equals mhdgb_set_boundary's bit for bit (values are only copied or negated).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -141,21 +143,52 @@ __global__ void k_fill_owned(double* __restrict__ P, Layout L, EdgeSnap S, int b
   }
 }
 
-// Address of g_edge_scratch on each device, resolved once per device on its first call.
+// Identity of the calling thread's current context, 0 if it cannot be read.  cudaDeviceReset (or
+// any other end of the primary context) destroys the context the scratch address was resolved in;
+// the context that replaces it loads the module again and may place g_edge_scratch elsewhere, and
+// it has a new identity.
+unsigned long long current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Address of g_edge_scratch on each device, resolved on the first call in each context of it.
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
-double* g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+  unsigned long long ctx_id;
+  double* addr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices] = {};
 
 cudaError_t scratch_address(int dev, double** out) {
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (dev < kMaxDevices && g_scratch_addr[dev]) {
-    *out = g_scratch_addr[dev];
+  const unsigned long long ctx = current_context_id();
+  if (dev < kMaxDevices && ctx != 0 && g_scratch_addr[dev].addr && g_scratch_addr[dev].ctx_id == ctx) {
+    *out = g_scratch_addr[dev].addr;
     return cudaSuccess;
   }
   void* p = nullptr;
   const cudaError_t e = cudaGetSymbolAddress(&p, g_edge_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < kMaxDevices) g_scratch_addr[dev] = static_cast<double*>(p);
+  if (dev < kMaxDevices) g_scratch_addr[dev] = ScratchAddr{current_context_id(), static_cast<double*>(p)};
   *out = static_cast<double*>(p);
   return cudaSuccess;
 }
@@ -179,6 +212,9 @@ extern "C" int mhdgb_fill_ghosts_noalloc(double* P, int nx, int ny, int nz, int 
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return MHDGB_ERR_CUDA;
+  // makes the device's primary context current on this thread (no allocation), so its identity can
+  // be read
+  if (cudaSetDevice(dev) != cudaSuccess) return MHDGB_ERR_CUDA;
   cudaPointerAttributes attr{};
   if (cudaPointerGetAttributes(&attr, P) != cudaSuccess) {
     cudaGetLastError();
@@ -201,7 +237,17 @@ extern "C" int mhdgb_fill_ghosts_noalloc(double* P, int nx, int ny, int nz, int 
   const int bs = 256;
   const long long nsnap = (long long)snapshot_doubles(nx, ny, nz);
   const long long nfill = (long long)NPRIM * (4LL * L.jtot * L.itot + 4LL * (nz + 1) * L.itot + 4LL * (nz + 1) * (ny + 1));
-  k_edge_snapshot<<<(unsigned)((nsnap + bs - 1) / bs), bs, 0, s>>>(P, L, S);
-  k_fill_owned<<<(unsigned)((nfill + bs - 1) / bs), bs, 0, s>>>(P, L, S, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5]);
-  return cudaGetLastError() == cudaSuccess ? MHDGB_OK : MHDGB_ERR_CUDA;
+  // cudaLaunchKernel returns the status of its own launch, so an error left pending by an earlier,
+  // unrelated call on this thread is neither reported as ours nor cleared
+  const double* Pc = P;
+  void* snap_args[] = {(void*)&Pc, (void*)&L, (void*)&S};
+  if (cudaLaunchKernel((const void*)k_edge_snapshot, dim3((unsigned)((nsnap + bs - 1) / bs)), dim3(bs), snap_args, 0,
+                       s) != cudaSuccess)
+    return MHDGB_ERR_CUDA;
+  int b[6] = {bc[0], bc[1], bc[2], bc[3], bc[4], bc[5]};
+  void* fill_args[] = {(void*)&P, (void*)&L, (void*)&S, &b[0], &b[1], &b[2], &b[3], &b[4], &b[5]};
+  if (cudaLaunchKernel((const void*)k_fill_owned, dim3((unsigned)((nfill + bs - 1) / bs)), dim3(bs), fill_args, 0,
+                       s) != cudaSuccess)
+    return MHDGB_ERR_CUDA;
+  return MHDGB_OK;
 }

@@ -34,8 +34,8 @@ cudaError_t launch_snapshot(const double* U, const double* P, const Layout& L, d
 // returns n, the number of HLLD tile variants out[0..n-1]; out[n] is the kind's run-time solver
 // kernel (HLLD, HLLE or HLLC from the arguments).
 int fused_variants(FusedKind kind, const FusedVariant** out);
-// The tile variant a grid starts with before any autotuning: the fastest measured on GB300 at the
-// benchmark sizes (150^3 and 256^3).
+// The tile variant a grid starts with before any autotuning: the table entry marked preferred (the
+// fastest measured on GB300 at the benchmark sizes, 150^3 and 256^3).
 int fused_preferred_variant(FusedKind kind);
 // Recover P (FP64 for FP64 kinds, FP32 for mixed) + ghost images from a.U into a.P[which];
 // reduce dt/c_h into slot.
@@ -46,8 +46,6 @@ namespace detail {
 int variants_exact(const FusedVariant** out);
 int variants_fp64(const FusedVariant** out);
 int variants_mixed(const FusedVariant** out);
-int preferred_fp64();
-int preferred_mixed();
 cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,
                           double* uh_ghost_out);
 cudaError_t recover_fp64(const FusedArgs& a, int which, RedSlot* slot, int nsm, cudaStream_t s, const double* uh_in,

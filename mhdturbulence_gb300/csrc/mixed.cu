@@ -11,8 +11,6 @@
 namespace mhdgb {
 namespace detail {
 
-int preferred_mixed() { return 6; }  // the fused-slope kernel, 16x8 cells, two CTAs per SM
-
 int variants_mixed(const FusedVariant** out) {
   static const FusedVariant v[] = {
       v_mixed::FusedLauncher<float, 32, 4, 128>::variant(FUSED_MIXED),
@@ -21,7 +19,7 @@ int variants_mixed(const FusedVariant** out) {
       v_mixed::FusedLauncher<float, 64, 4, 256>::variant(FUSED_MIXED),
       v_mixed::FusedLauncher<float, 32, 4, 256, 2>::variant(FUSED_MIXED),
       v_mixed::FusedLauncher<float, 16, 8, 256, 2>::variant(FUSED_MIXED),
-      v_mixed::FusedLauncherFS<16, 8, 256, 2>::variant(FUSED_MIXED),
+      preferred_variant(v_mixed::FusedLauncherFS<16, 8, 256, 2>::variant(FUSED_MIXED)),
       // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
       v_mixed::FusedLauncherFS<16, 8, 256, 2, true>::variant(FUSED_MIXED),
   };

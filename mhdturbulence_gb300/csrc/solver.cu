@@ -94,6 +94,9 @@ __global__ void k_ctrl_restore(Ctrl* c, unsigned long long step, double time, do
 // Point the step's host copy of U at v (null: none), in the launch descriptor on the device.
 __global__ void k_set_host_u(InstanceDesc* d, double* v) { d->a.Uh = v; }
 
+// Test hook of the abort self-test: extra bytes the first plane load of each work item expects.
+__global__ void k_set_tx_extra(InstanceDesc* d, unsigned v) { d->a.tx_extra = v; }
+
 // Failure-detection self-test: one thread waits on an mbarrier that no arrival or copy ever
 // completes.  The bounded wait (the one the fused step uses for its plane loads) gives up, sets
 // ST_TIMEOUT in *status, and the kernel returns normally.
@@ -1231,6 +1234,13 @@ int mhdgb_variant_info(const mhdgb_solver* h, int idx, int* tx, int* ty, int* th
   return MHDGB_OK;
 }
 
+const char* mhdgb_variant_name(const mhdgb_solver* h, int idx) {
+  if (!h) return nullptr;
+  if (idx == -1) idx = h->vidx;
+  if (idx < 0 || idx > h->nvars) return nullptr;
+  return h->vars[idx].name;
+}
+
 int mhdgb_select_variant(mhdgb_solver* h, int idx) {
   if (!h || idx < 0 || idx >= h->nvars) return MHDGB_ERR_ARG;
   int rc = set_device(h);
@@ -1342,6 +1352,56 @@ int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, doubl
         U[at(mst)] = rho * X;
       }
   return mhdgb_upload_cons(h, U.data());
+}
+
+int mhdgb_selftest_fused_abort(int device, int precision, double* seconds, unsigned* status, int* recovered) {
+  if (!seconds || !status || !recovered) return MHDGB_ERR_ARG;
+  if (precision < MHDGB_FP64 || precision > MHDGB_MIXED) return MHDGB_ERR_ARG;
+  mhdgb_config cfg;
+  mhdgb_config_default(&cfg);
+  cfg.nx = 32; cfg.ny = 24; cfg.nz = 16;
+  cfg.precision = precision;
+  cfg.device = device;
+  mhdgb_solver *h = nullptr, *ref = nullptr;
+  int rc = mhdgb_create(&cfg, &h);
+  if (rc) return rc;
+  if ((rc = mhdgb_create(&cfg, &ref))) { mhdgb_destroy(h); return rc; }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto done = [&](int code) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    mhdgb_destroy(h);
+    mhdgb_destroy(ref);
+    return code;
+  };
+  auto init = [](mhdgb_solver* s) { return mhdgb_init_kh(s, 1, 0.5, 0.05, 0.1, 1e-2, 0.2, 1e-4); };
+  if ((rc = init(h)) || (rc = mhdgb_prepare(h))) return done(rc);
+  // one step whose first plane load per work item expects 16 bytes more than the plane: every CTA
+  // with a work item waits for that plane until the bounded wait gives up, then drains and returns
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return done(MHDGB_ERR_CUDA);
+  k_set_tx_extra<<<1, 1, 0, h->stream>>>(h->d_desc, 16u);
+  if (cudaGetLastError() != cudaSuccess || cudaEventRecord(e0, h->stream) != cudaSuccess) return done(MHDGB_ERR_CUDA);
+  if ((rc = launch_one(h))) return done(rc);
+  if (cudaEventRecord(e1, h->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+    return done(MHDGB_ERR_CUDA);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  Ctrl c;
+  if ((rc = read_ctrl(h, &c))) return done(rc);
+  *seconds = ms * 1e-3;
+  *status = c.status;
+  // the same handle then runs two ordinary steps from a fresh state, which must equal a handle that
+  // never saw the aborted launch bit for bit
+  k_set_tx_extra<<<1, 1, 0, h->stream>>>(h->d_desc, 0u);
+  if (cudaGetLastError() != cudaSuccess) return done(MHDGB_ERR_CUDA);
+  if ((rc = mhdgb_reset_clock(h)) || (rc = init(h)) || (rc = mhdgb_step(h, 2))) return done(rc);
+  const int sync_rc = mhdgb_sync(h, nullptr);
+  if ((rc = init(ref)) || (rc = mhdgb_step(ref, 2)) || (rc = mhdgb_sync(ref, nullptr))) return done(rc);
+  const size_t n = (size_t)NCONS * h->L.itot * h->L.jtot * h->L.ktot;
+  std::vector<double> a(n), b(n);
+  if ((rc = mhdgb_download_cons(h, a.data())) || (rc = mhdgb_download_cons(ref, b.data()))) return done(rc);
+  *recovered = sync_rc == MHDGB_OK && std::memcmp(a.data(), b.data(), n * sizeof(double)) == 0;
+  return done(MHDGB_OK);
 }
 
 }  // extern "C"

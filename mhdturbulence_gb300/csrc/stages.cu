@@ -348,7 +348,7 @@ cudaError_t launch_ghost_fill(double* P, const Layout& L, const int bc[6], doubl
 namespace detail {
 int variants_exact(const FusedVariant** out) {
   static const FusedVariant v[] = {
-      v_exact::FusedLauncher<double, 32, 4, 128>::variant(FUSED_FP64_EXACT),
+      preferred_variant(v_exact::FusedLauncher<double, 32, 4, 128>::variant(FUSED_FP64_EXACT)),
       // the run-time solver kernel (HLLE / HLLC); not one of the tuned variants
       v_exact::FusedLauncher<double, 32, 4, 128, 1, true>::variant(FUSED_FP64_EXACT),
   };
@@ -362,11 +362,11 @@ cudaError_t recover_exact(const FusedArgs& a, int which, RedSlot* slot, int nsm,
 }  // namespace detail
 
 int fused_preferred_variant(FusedKind kind) {
-  switch (kind) {
-    case FUSED_FP64_EXACT: return 0;
-    case FUSED_FP64: return detail::preferred_fp64();
-    default: return detail::preferred_mixed();
-  }
+  const FusedVariant* v = nullptr;
+  const int n = fused_variants(kind, &v);
+  for (int i = 0; i < n; i++)
+    if (v[i].preferred) return i;
+  return 0;
 }
 
 int fused_variants(FusedKind kind, const FusedVariant** out) {

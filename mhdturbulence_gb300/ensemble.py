@@ -119,6 +119,11 @@ class Ensemble:
     def variant(self) -> int:
         return int(self._L.mhdgb_ensemble_variant(self._e))
 
+    @property
+    def variant_name(self) -> str:
+        """Kernel form and tile shape every member runs."""
+        return self.members[0].variant_name(-1)
+
     def autotune(self, steps=2) -> int:
         best = C.c_int()
         self._ck(self._L.mhdgb_ensemble_autotune(self._e, steps, C.byref(best)), "autotune")

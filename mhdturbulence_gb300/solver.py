@@ -231,6 +231,13 @@ class Solver:
             out.append((tx.value, ty.value, nt.value, bool(cur.value)))
         return out
 
+    def variant_name(self, idx=-1) -> str:
+        """Kernel form and tile shape of variant idx (-1: the kernel in use)."""
+        name = self._L.mhdgb_variant_name(self._h, idx)
+        if name is None:
+            raise MhdgbError(-1, f"variant_name: no variant {idx}")
+        return name.decode()
+
     def select_variant(self, idx):
         self._ck(self._L.mhdgb_select_variant(self._h, idx), "select_variant")
 

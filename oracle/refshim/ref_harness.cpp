@@ -65,6 +65,7 @@ int main(int argc, char** argv) {
   FILE* out = std::fopen(argv[2], "wb");
   if (!out) fail("cannot open output");
   std::vector<double> P1, U1, F1;
+  const auto t0 = std::chrono::steady_clock::now();
   for (int step = 0; step < nsteps; step++) {
     ControlTimestep(G);
     boundary_mod::SetBoundaryCondition(P, boundary_mod::Bs, boundary_mod::Br);
@@ -88,6 +89,10 @@ int main(int argc, char** argv) {
       }
     }
   }
+  // wall time of the step loop (the first step's copies of P, U and F included), reported the way
+  // the reference's main.cpp:274-276 does
+  const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::fprintf(stderr, "time/count/cell : %e\n", wall / ((double)ngrid1 * ngrid2 * ngrid3) / nsteps);
   std::fwrite(dts.data(), sizeof(double), nsteps, out);
   std::fwrite(chgs.data(), sizeof(double), nsteps, out);
   std::fwrite(P0.data(), sizeof(double), P0.size(), out);

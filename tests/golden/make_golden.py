@@ -131,7 +131,8 @@ def make_output_golden(refdir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--refdir", default="/root/reference/src_cpp_kokkos_host")
+    ap.add_argument("--refdir", default=os.environ.get("MHDTURB_REFDIR"), required="MHDTURB_REFDIR" not in os.environ,
+                    help="the reference's src_cpp_kokkos_host directory (or set MHDTURB_REFDIR)")
     ap.add_argument("--only", choices=["stages", "output"], default=None)
     args = ap.parse_args()
     if args.only != "stages":

@@ -83,3 +83,54 @@ def test_ensemble_stop_condition_per_member():
         reps = ens.sync()
         assert [r.step for r in reps] == [4, 2, 4]
         assert all(r.done for r in reps)
+
+
+def test_ensemble_members_exact_vs_oracle():
+    """Each member of an uneven ensemble in the separately rounded FP64 form equals the oracle (the
+    reference's stage arithmetic bit for bit) run on that member's grid: state, time and every
+    step's dt and c_h."""
+    import oracle as O
+
+    specs = kh_ensemble_specs(4, seed=11, sizes=(12, 20, 28))
+    specs[0]["bc"] = (ic.BC_REFLECTION, ic.BC_OUTFLOW, ic.BC_PERIODIC, ic.BC_PERIODIC, ic.BC_OUTFLOW,
+                      ic.BC_REFLECTION)
+    specs[2]["bc"] = ic.PERIODIC_BC
+    specs[2]["domain"] = ic.CUBE_DOMAIN
+    nsteps = 12
+    with Ensemble(specs, precision="fp64_exact") as ens:
+        ens.init_kh()
+        U0 = [m.download_cons() for m in ens.members]
+        got_dt = [[] for _ in specs]
+        for _ in range(nsteps):
+            ens.step(1)
+            for q, r in enumerate(ens.sync()):
+                got_dt[q].append((r.dt, r.chg))
+        reps = ens.sync()
+        out = [ic.interior(m.download_cons()) for m in ens.members]
+    for q, (sp, u0) in enumerate(zip(specs, U0)):
+        nx, ny, nz = sp["nx"], sp["ny"], sp["nz"]
+        domain, bc = sp.get("domain", ic.KH_DOMAIN), sp.get("bc", ic.KH_BC)
+        orc = O.Oracle(nx, ny, nz, *ic.grid(nx, ny, nz, domain), gam=5.0 / 3.0, bc=bc, spacing_quirk=False)
+        U, P = u0.copy(), ic.empty_field(nx, ny, nz, 12)
+        orc.update_prim(U, P)
+        t, dts, chgs = orc.run(U, P, nsteps)
+        assert np.array_equal(out[q], ic.interior(U)), q
+        assert got_dt[q] == list(zip(dts.tolist(), chgs.tolist())), q
+        assert reps[q].time == t, q
+
+
+def test_new_grids_start_on_the_preferred_kernels():
+    """Before any autotuning a grid or ensemble starts on the table entry marked as the fastest
+    measured at the benchmark sizes: the two-phase 16x8/256 kernel in FP64 and the fused-slope
+    16x8/256 kernel compiled for two CTAs per SM in the mixed form; HLLE/HLLC run on the run-time
+    solver kernel."""
+    want = {"fp64": "two-phase 16x8/256", "mixed": "fused-slope 16x8/256 x2", "fp64_exact": "two-phase 32x4/128"}
+    for precision, name in want.items():
+        with Solver(150, 150, 150, precision=precision) as s:
+            assert s.variant_name() == name, precision
+            s.set_riemann("hllc")
+            assert s.variant_name().endswith("run-time solver"), precision
+            s.set_riemann("hlld")
+            assert s.variant_name() == name, precision
+        with Ensemble(kh_ensemble_specs(3, seed=5, sizes=(16, 24)), precision=precision) as ens:
+            assert ens.variant_name == name, precision

@@ -26,9 +26,10 @@ CASES = [
 ]
 
 
-def _fill(P, nx, ny, nz, pitch, bc):
+def _fill(P, nx, ny, nz, pitch, bc, stream=None):
     bcs = (C.c_int * 6)(*bc)
-    stream = torch.cuda.current_stream().cuda_stream
+    if stream is None:
+        stream = torch.cuda.current_stream().cuda_stream
     return _lib.lib().mhdgb_fill_ghosts_noalloc(P.data_ptr(), nx, ny, nz, pitch, bcs, stream)
 
 
@@ -63,6 +64,36 @@ def test_matches_set_boundary_on_two_calls_in_a_row(shape, bc, pad):
     assert np.array_equal(got1[..., :itot], want1)
     assert np.array_equal(got2[..., :itot], want2)
     assert np.array_equal(got2[..., itot:], host[..., itot:])   # row padding untouched
+
+
+def test_on_a_caller_stream_without_allocating():
+    """The use the entry point is for: a caller's own (non-default) stream, with the device's free
+    memory the same before and after two calls.  Only that stream is synchronised before the
+    result is read, so the two kernels of each call must run in order on it."""
+    nx, ny, nz, bc = 20, 14, 10, (1, 1, 2, 2, 3, 1)
+    itot, jtot, ktot = nx + 5, ny + 5, nz + 5
+    rng = np.random.default_rng(7)
+    P0 = rng.standard_normal((ktot, jtot, NPRIM, itot)) + 2.0
+    with Solver(nx, ny, nz, bc=bc, precision="fp64_exact") as s:
+        s.upload_prim(P0)
+        s.SetBoundaryCondition()
+        s.SetBoundaryCondition()
+        want = s.download_prim()
+
+    P = torch.from_numpy(P0).to("cuda")
+    # the first call on a device loads the module, whose static scratch is then resident
+    assert _fill(P, nx, ny, nz, 0, bc) == 0
+    P.copy_(torch.from_numpy(P0))
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    assert _fill(P, nx, ny, nz, 0, bc, stream.cuda_stream) == 0
+    assert _fill(P, nx, ny, nz, 0, bc, stream.cuda_stream) == 0
+    stream.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    got = P.cpu().numpy()
+    assert free_after == free_before
+    assert np.array_equal(got, want)
 
 
 def test_rejects_requests_it_cannot_serve():
