@@ -13,16 +13,22 @@ Prints one JSON line.  value = whole-job Gcell-updates/s of the FP64 form with t
 in HBM (CUDA events on the launching stream, W warm-up steps, then K timed steps; the 150^3 state
 is ~1 GB, larger than L2, so no flush is needed); e2e = the same through mhdgb_step_host with the
 state in pinned host memory, moved in and out every step (298 MB each way over the host link);
-"mixed" = the FP32-mixed form on the same
-configuration with its error against the FP64 form; cpu_baseline = the oracle (the reference's
+"mixed" = the FP32-mixed form on the same configuration, with its own e2e and its error against
+the FP64 form; "size_256" = both forms on KH 256^3 (the size the FP64-roofline and mixed-speed-up
+targets are quoted at); "ensemble" = 64 seeded uneven KH grids in one persistent launch per step,
+mixed and FP64, against one 512^3 mixed grid; cpu_baseline = the oracle (the reference's
 arithmetic restated in C, OpenMP) on this host's cores.
 
 --impl reference times the reference's CPU path on the host cores: the reference sources cannot
 be built on this machine (they need Kokkos and MPI, and the reference tree is absent here), so the
-oracle port stands in for it, with all host threads.
+oracle port stands in for it, with all host threads.  On the same cores the port runs 1.34x as fast
+as the reference's own stages built against a Kokkos/MPI shim (oracle/cpu_baseline_fidelity.py),
+so the ratio against this arm understates the speed-up over the reference itself.
 
-Multi-GPU (torchrun): every rank advances its own independent 150^3 replica ("replicas only": the
-path has no exchange here), timings are max-reduced over ranks, value sums all ranks.
+Multi-GPU (torchrun): the ranks hold the 150^3 blocks of one 150 x 150 x (150 N) KH grid split
+along z and swap the halos of their shared faces over NCCL after every step, with dt and c_h
+all-reduced (mhdturbulence_gb300.distributed; weak scaling); timings are max-reduced over ranks,
+value sums all ranks.
 """
 from __future__ import annotations
 
@@ -190,8 +196,7 @@ def run_reference(args, ws, rank):
         "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "ns_per_cell_step": 1.0 / rate,
-        "config": {"workload": f"Kelvin-Helmholtz {args.n}^3, FP64, CFL factor 0.05 (reference benchmark problem)",
-                   "cells": args.n ** 3},
+        "config": bench_config(args.n, ws),
         "cpu_baseline": {"value": rate, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": rate, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -252,8 +257,153 @@ def run_only(args, local):
                       "status": int(r.status)}), flush=True)
 
 
+def bench_config(n, ws):
+    """The workload description both arms print (identical dicts)."""
+    par = "1 GPU" if ws == 1 else f"{ws} blocks of one {n}x{n}x{n * ws} grid (z split), halos exchanged every step"
+    return {"workload": f"Kelvin-Helmholtz {n}^3, FP64, CFL factor 0.05 (reference benchmark problem)",
+            "cells_per_gpu": n ** 3, "parallelism": par,
+            "l2": "inputs larger than L2 (state ~1 GB per GPU); no flush"}
+
+
+def timed(solver_like, steps, warm, local):
+    """(ms over `steps` steps, clocks) of a Solver / Ensemble after `warm` untimed steps."""
+    solver_like.time_steps(max(1, warm))
+    with Clocks(local) as ck:
+        ms = solver_like.time_steps(steps)
+    return ms, ck.summary()
+
+
+def hbm_roofline(cells, ms_step, hbm_peak, limiter, traffic_per_cell=None):
+    ach = B_ALG * cells / (ms_step * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+            "traffic": traffic_per_cell * cells if traffic_per_cell else None, "limiter": limiter}
+
+
+def e2e_leg(n, precision, K, ws, local):
+    """The same metric end to end through mhdgb_step_host: pinned host U in and out every step."""
+    import torch
+    from mhdturbulence_gb300 import Solver
+    with Solver(n, n, n, precision=precision, device=local) as s:
+        s.init_kh(seed=1)
+        U0 = s.download_cons()
+        hin = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True)
+        hout = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True)
+        hin.numpy()[...] = U0
+        a, b = hin.numpy(), hout.numpy()
+        s.step_host(a, b, 1)
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(K):
+            s.step_host(a, b, 1)
+            a, b = b, a
+        el = allmax(ws, time.perf_counter() - t0)
+    return {"value": replica_value(ws, n ** 3, K, el * 1e3), "unit": "Gcell-updates/s",
+            "h2d_bytes_per_step": U0.nbytes, "d2h_bytes_per_step": U0.nbytes,
+            "api": "mhdgb_step_host (pinned host U in/out, 1 step per call)", "ms_per_step": el / K * 1e3}
+
+
+def size_leg(n, K, W, hbm_peak, local):
+    """FP64 and mixed KH n^3 on the preferred kernels (no autotuning)."""
+    from mhdturbulence_gb300 import Solver
+    out = {}
+    for prec, k in (("fp64", K), ("mixed", 8 * K)):
+        with Solver(n, n, n, precision=prec, device=local) as s:
+            s.init_kh(seed=1)
+            ms, ck = timed(s, k, W, local)
+            r = s.sync()
+            cells = n ** 3
+            out[prec] = {"value": cells * k / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s", "ms_per_step": ms / k,
+                         "ns_per_cell_step": ms / k * 1e6 / cells, "steps": k, "kernel": s.variant_name(),
+                         "status": int(r.status), "clocks": ck,
+                         "roofline": hbm_roofline(cells, ms / k, hbm_peak,
+                                                  "fp64_pipe" if prec == "fp64" else "instruction issue")}
+    out["mixed_speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def ensemble_leg(K, W, local, members=64):
+    """The batched form: 64 seeded uneven KH grids (per-axis extents from {32, 48, 64, 96, 128}, shear
+    Mach U[0.3, 1.5], B_x U[0, 0.3], own noise seeds) in one persistent launch per step, against one
+    512^3 KH grid in the mixed form."""
+    from mhdturbulence_gb300 import Ensemble, Solver, kh_ensemble_specs
+    specs = kh_ensemble_specs(members, seed=2026)
+    out = {"members": members, "grids": "per-axis extents from {32,48,64,96,128}, <= 128^3 cells each"}
+    for prec, k in (("mixed", 4 * K), ("fp64", max(2, K // 4))):
+        with Ensemble(specs, precision=prec, device=local) as ens:
+            ens.init_kh()
+            ms, ck = timed(ens, k, W, local)
+            ens.sync()
+            cells = ens.cells
+            out["cells"] = cells
+            out[prec] = {"value": cells * k / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s", "ms_per_step": ms / k,
+                         "steps": k, "kernel": ens.variant_name, "clocks": ck}
+    n = 512
+    with Solver(n, n, n, precision="mixed", device=local) as s:
+        s.init_kh(seed=1)
+        k = 2 * K
+        ms, ck = timed(s, k, W, local)
+        out["single_512_mixed"] = {"value": n ** 3 * k / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+                                   "ms_per_step": ms / k, "steps": k, "clocks": ck}
+    out["mixed_frac_of_single_512"] = out["mixed"]["value"] / out["single_512_mixed"]["value"]
+    return out
+
+
+def run_decomposed(args, ws, rank, local):
+    """N > 1: one KH grid of n x n x (n*N) cells (z in [-N/2, N/2], periodic), one n^3 block per
+    rank (mhdturbulence_gb300.distributed), halos of the shared z faces swapped after every step and
+    dt / c_h all-reduced: weak scaling with the path's own exchange step.  Halos move over NCCL
+    between GPUs (--halo-transport gloo: page-locked host buffers over gloo)."""
+    import torch
+    import torch.distributed as dist
+    from mhdturbulence_gb300.distributed import DistributedGrid, GpuBlock
+    dev = local if args.halo_transport == "nccl" else args.device
+    torch.cuda.set_device(dev)
+    group = dist.new_group(backend="nccl") if args.halo_transport == "nccl" else None
+    n, K, W = args.n, args.steps, args.warmup
+    nz = n * ws
+    domain = ((-0.5, 0.5), (-1.0, 1.0), (-0.5 * ws, 0.5 * ws))
+    res = {}
+    for prec, k in (("fp64", K), ("mixed", K * args.mixed_factor)):
+        blk = GpuBlock(n, n, nz, (1, 1, ws), (0, 0, rank), domain=domain, precision=prec, device=dev,
+                       transport="cuda" if args.halo_transport == "nccl" else "cpu")
+        blk.init_kh(seed=1)
+        g = DistributedGrid(blk, group=group)
+        g.prepare()
+        g.step(W)
+        torch.cuda.synchronize(dev)
+        with Clocks(dev) as ck:
+            barrier(ws)
+            t0 = time.perf_counter()
+            g.step(k)
+            torch.cuda.synchronize(dev)
+            el = allmax(ws, time.perf_counter() - t0)
+        r = g.sync()
+        res[prec] = {"value": ws * n ** 3 * k / el / 1e9, "ms_per_step": el / k * 1e3, "steps": k,
+                     "clocks": ck.summary(), "status": int(r.status), "kernel": blk.solver.variant_name()}
+        blk.solver.close()
+    e2e = e2e_leg(n, "fp64", max(2, K // 2), ws, dev)
+    if rank != 0:
+        return
+    hbm_peak, peak_kind = peaks()
+    fp, mx = res["fp64"], res["mixed"]
+    roofline = hbm_roofline(n ** 3, fp["ms_per_step"], hbm_peak, "fp64_pipe")
+    roofline["peak_kind"] = peak_kind
+    line = {
+        "metric": METRIC, "value": fp["value"], "unit": "Gcell-updates/s", "n_gpus": ws, "steps": fp["steps"],
+        "warmup": W, "ms_per_step": fp["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded KH initial state, mhdgb_init_kh_block)",
+        "kernel": fp["kernel"], "config": bench_config(n, ws), "roofline": roofline,
+        "mixed": {"value": mx["value"], "unit": "Gcell-updates/s", "ms_per_step": mx["ms_per_step"],
+                  "clocks": mx["clocks"], "kernel": mx["kernel"]},
+        "e2e": dict(e2e, api=e2e["api"] + "; each rank's block as an independent grid"),
+        "gpu_launches": fp["steps"], "clocks": fp["clocks"], "status": fp["status"], "cpu_baseline": None,
+        "halo_transport": args.halo_transport,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, ws, rank, local):
-    from mhdturbulence_gb300 import Solver, ic, _lib
+    from mhdturbulence_gb300 import Solver, _lib
 
     n, K, W = args.n, args.steps, args.warmup
     cells = n ** 3
@@ -264,8 +414,8 @@ def run_ours(args, ws, rank, local):
         kk = K if prec == "fp64" else K * args.mixed_factor
         with Solver(n, n, n, precision=prec, device=local) as s:
             s.init_kh(seed=1)
-            best = s.autotune(steps=2)
-            tx, ty, nt, _ = s.variants()[best]
+            s.autotune(steps=2)
+            name = s.variant_name()
             s.time_steps(W)
             barrier(ws)
             with Clocks(local) as ck:
@@ -275,49 +425,25 @@ def run_ours(args, ws, rank, local):
             ms_max = allmax(ws, ms)
             if prec == "fp64":
                 launches = kk
-            res[prec] = {"ms": ms_max, "steps": kk, "tile": f"{tx}x{ty}/{nt}", "clocks": ck.summary(),
+            res[prec] = {"ms": ms_max, "steps": kk, "kernel": name, "clocks": ck.summary(),
                          "status": int(r.status), "device_bytes": s.device_bytes}
-            log(f"[bench] {prec}: {ms_max / kk:.3f} ms/step, tile {tx}x{ty}/{nt}")
+            log(f"[bench] {prec}: {ms_max / kk:.3f} ms/step, {name}")
 
-    # end to end through the C ABI with the state in pinned host memory, copied in and out every step
-    import torch
-    e2e = None
-    with Solver(n, n, n, precision="fp64", device=local) as s:
-        s.init_kh(seed=1)
-        U0 = s.download_cons()
-        hin = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True)
-        hout = torch.empty(U0.shape, dtype=torch.float64, pin_memory=True)
-        hin.numpy()[...] = U0
-        a, b = hin.numpy(), hout.numpy()
-        ke = max(2, K // 2)
-        s.step_host(a, b, 1)
-        barrier(ws)
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            s.step_host(a, b, 1)
-            a, b = b, a
-        el = time.perf_counter() - t0
-        el = allmax(ws, el)
-        nbytes = U0.nbytes
-        e2e = {"value": replica_value(ws, cells, ke, el * 1e3), "unit": "Gcell-updates/s", "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "api": "mhdgb_step_host (pinned host U in/out, 1 step per call)",
-               "ms_per_step": el / ke * 1e3}
+    e2e = e2e_leg(n, "fp64", max(2, K // 2), ws, local)
+    e2e_mixed = e2e_leg(n, "mixed", max(4, K), ws, local)
 
     if rank != 0:
         return
     fp = res["fp64"]
     ms_step = fp["ms"] / fp["steps"]
     value = replica_value(ws, cells, fp["steps"], fp["ms"])
-    achieved = B_ALG * cells / (ms_step * 1e-3) / 1e9
     prof = profile_summary("fused_fp64_150.json")
-    traffic = None
-    if prof and prof.get("dram_bytes_per_cell"):
-        traffic = prof["dram_bytes_per_cell"] * cells
+    traffic = prof.get("dram_bytes_per_cell") if prof else None
     # "bound"/"frac": the HBM roofline of the contract; "limiter": what actually bounds the kernel (the
     # FP64 pipe, whose use is reported under fp64_pipe)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": traffic, "peak_kind": peak_kind, "limiter": "fp64_pipe",
-                "kernel": "k_fused_step<double> (one launch per step)", "bytes_per_cell_alg": B_ALG}
+    roofline = hbm_roofline(cells, ms_step, hbm_peak, "fp64_pipe", traffic)
+    roofline.update({"peak_kind": peak_kind, "kernel": "k_fused_step<double> (one launch per step)",
+                     "bytes_per_cell_alg": B_ALG})
     fp64_rate = None
     rate = ctypes.c_double()
     if _lib.lib().mhdgb_measure_fp64_rate(local, ctypes.byref(rate)) == 0:
@@ -343,15 +469,12 @@ def run_ours(args, ws, rank, local):
     mx = res["mixed"]
     mx_step = mx["ms"] / mx["steps"]
     mx_value = replica_value(ws, cells, mx["steps"], mx["ms"])
-    mx_achieved = B_ALG * cells / (mx_step * 1e-3) / 1e9
     prof_m = profile_summary("fused_mixed_150.json")
     mixed = {"value": mx_value, "unit": "Gcell-updates/s", "ns_per_cell_step": 1.0 / mx_value * ws,
-             "ms_per_step": mx_step, "speedup_vs_fp64": mx_value / value, "tile": mx["tile"],
-             "roofline": {"bound": "hbm", "achieved": mx_achieved, "peak": hbm_peak, "unit": "GB/s",
-                          "frac": mx_achieved / hbm_peak, "limiter": "instruction issue (see issue)",
-                          "traffic": (prof_m["dram_bytes_per_cell"] * cells) if prof_m and
-                          prof_m.get("dram_bytes_per_cell") else None},
-             "clocks": mx["clocks"]}
+             "ms_per_step": mx_step, "speedup_vs_fp64": mx_value / value, "kernel": mx["kernel"],
+             "roofline": hbm_roofline(cells, mx_step, hbm_peak, "instruction issue (see issue)",
+                                      prof_m.get("dram_bytes_per_cell") if prof_m else None),
+             "clocks": mx["clocks"], "e2e": e2e_mixed}
     if prof_m and prof_m.get("warp_inst_per_cell") and mx["clocks"].get("sm_mhz"):
         # the mixed step's bound is instruction issue: the warp instructions per cell (ncu) against
         # one warp instruction per clock per SM sub-partition (4 per SM) at the sampled SM clock
@@ -363,6 +486,14 @@ def run_ours(args, ws, rank, local):
                           "frac": ach / peak, "warp_inst_per_cell": prof_m["warp_inst_per_cell"]}
     if not args.no_error:
         mixed["error_vs_fp64"] = mixed_error(n, args.error_steps, local)
+    extra = {}
+    if not args.no_extra:
+        extra["size_256"] = size_leg(256, max(4, K // 3), W, hbm_peak, local)
+        log(f"[bench] 256^3: fp64 {extra['size_256']['fp64']['ms_per_step']:.3f} ms/step, "
+            f"mixed {extra['size_256']['mixed']['ms_per_step']:.3f} ms/step")
+        extra["ensemble"] = ensemble_leg(K, W, local)
+        log(f"[bench] ensemble: mixed {extra['ensemble']['mixed']['value']:.3f} Gcell/s = "
+            f"{extra['ensemble']['mixed_frac_of_single_512']:.3f} of one 512^3 grid")
     cpu = None
     if ws == 1 and not args.no_cpu:
         crate, threads, csteps, cel = cpu_oracle_rate(n, args.cpu_seconds)
@@ -372,11 +503,9 @@ def run_ours(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": ws, "steps": fp["steps"],
         "warmup": W, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded KH initial state, mhdgb_init_kh)",
-        "ns_per_cell_step": ms_step * 1e6 / cells,
-        "config": {"workload": f"Kelvin-Helmholtz {n}^3, FP64, CFL factor 0.05 (reference benchmark problem)",
-                   "cells_per_gpu": cells, "tile": fp["tile"], "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (state ~1 GB per replica); no flush"},
-        "roofline": roofline, "fp64_pipe": fp64_pipe, "mixed": mixed, "cpu_baseline": cpu, "e2e": e2e,
+        "ns_per_cell_step": ms_step * 1e6 / cells, "kernel": fp["kernel"],
+        "config": bench_config(n, ws),
+        "roofline": roofline, "fp64_pipe": fp64_pipe, "mixed": mixed, **extra, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": fp["clocks"], "status": fp["status"],
         "published_context": {"value": 1e-9 / PUBLISHED_4XA100_S_PER_CELL_STEP, "unit": "Gcell-updates/s",
                               "what": "4x A100, f90 OpenACC, 150^3 to t=15 (reference README.md:95)"},
@@ -399,6 +528,10 @@ def main():
     ap.add_argument("--cpu-seconds-ref", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the 256^3, ensemble and 512^3 legs")
+    ap.add_argument("--halo-transport", choices=["nccl", "gloo"], default="nccl",
+                    help="N > 1: halos over NCCL between GPUs, or over gloo through host memory")
+    ap.add_argument("--device", type=int, default=0, help="N > 1 with gloo halos: the GPU every rank uses")
     ap.add_argument("--only", choices=["fp64", "mixed", "fp64_exact"], help="time one form only (profiling)")
     ap.add_argument("--variant", type=int, default=0, help="tile-shape variant for --only")
     args = ap.parse_args()
@@ -408,6 +541,8 @@ def main():
         run_only(args, local)
     elif args.impl == "reference":
         run_reference(args, ws, rank)
+    elif ws > 1:
+        run_decomposed(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -41,6 +41,10 @@ extern "C" {
 #define MHDGB_BC_PERIODIC 1
 #define MHDGB_BC_REFLECTION 2
 #define MHDGB_BC_OUTFLOW 3
+/* A face shared with another block of a decomposed grid (the reference's MPI neighbours,
+ * mpi_config.cpp:61-69): no local fill writes its ghost layers, which the halo exchange copies from
+ * the neighbour (mhdgb_halo_pack / _unpack, or a domain's own exchange); boundary.cpp:222-318. */
+#define MHDGB_BC_EXCHANGE 4
 
 /* precision of the fused step */
 #define MHDGB_FP64 0        /* FP64 throughout, FMA contraction (last-bit differences) */
@@ -185,6 +189,11 @@ int mhdgb_select_variant(mhdgb_solver* h, int idx);
  * (x2: compiled for two CTAs per SM); idx = -1 names the kernel in use, which for HLLE/HLLC is the
  * run-time solver kernel.  NULL for an invalid index. */
 const char* mhdgb_variant_name(const mhdgb_solver* h, int idx);
+/* Work decomposition of the fused step in use: tiles per axis, z chunks per tile column and, if
+ * kstart is not NULL, the nchunks + 1 chunk boundaries (interior plane indices, 0 .. nz).  The work
+ * queue hands out chunk 0 of every tile first; chunks that shrink towards the end of the queue even
+ * out the CTAs' finish times. */
+int mhdgb_work_layout(const mhdgb_solver* h, int* ntx, int* nty, int* nchunks, int* kstart);
 /* Time every compiled tile shape on the handle's grid (steps fused steps each, from the current
  * state, which is restored afterwards) and keep the fastest.  The choice is remembered per
  * (precision, nx, ny, nz) for later handles in the process and, if the environment variable
@@ -223,6 +232,12 @@ int mhdgb_diag(mhdgb_solver* h, double out[3]);
  * scalar X = (1+tanh(y/width))/2) written into U; see mhdturbulence_gb300/ic.py. */
 int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, double width, double bx, double amp,
                   double sig, double noise);
+/* The same state for a block of a decomposed grid: the handle's cells are cells offset[a] ..
+ * offset[a] + n[a] - 1 of a whole grid of whole[0] x whole[1] x whole[2] cells, whose seeded noise
+ * they take (so the blocks together hold exactly the single grid's state).  The handle's cell faces
+ * must already be the whole grid's (mhdgb_set_grid). */
+int mhdgb_init_kh_block(mhdgb_solver* h, const int whole[3], const int offset[3], unsigned long long seed,
+                        double vshear, double width, double bx, double amp, double sig, double noise);
 
 /* ---- snapshot output ----
  * Output(true) of src_cpp_kokkos_host/output.cpp:379-407 for one rank: under root (NULL: "."),
@@ -305,6 +320,79 @@ int mhdgb_ensemble_autotune(mhdgb_ensemble* e, int steps, int* best);
 #define MHDGB_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define MHDGB_NOALLOC_MAX_EXTENT_SUM 2723
 int mhdgb_fill_ghosts_noalloc(double* P, int nx, int ny, int nz, int pitch, const int* bc, void* stream);
+
+/* ---- block decomposition (replaces the MPI topology and halo exchange of the reference) ----
+ * The reference splits the grid over MPI ranks (MPI_Cart_create, mpi_config.cpp:61-69), exchanges
+ * 2-deep primitive halos with its neighbours in SendRecvBoundary (boundary.cpp:222-318, 430-475,
+ * 627-672, MPI_Waitall at :715) and reduces dt and c_h over ranks (MPIminfind / MPImaxfind,
+ * mpi_config.cpp:83-99).  A block here is an ordinary handle whose faces shared with another block
+ * have the kind MHDGB_BC_EXCHANGE.  Faces are numbered 0..5 = x-in, x-out, y-in, y-out, z-in, z-out;
+ * a halo is the 12 primitives of the 2 cell layers next to a face over the face's interior extent,
+ * ordered i fastest, then j, k and the variable.  Only that extent is exchanged: the solver never
+ * reads the edge and corner ghosts.
+ *
+ * Per handle (one process per GPU, the caller's own transport, e.g. MPI or NCCL): after
+ * mhdgb_prepare or a step, pack the layers next to each exchanged face, send them to the
+ * neighbour, unpack what the neighbours sent into the ghost layers, replace the pending reduction
+ * by its minimum / maximum over all blocks, and step once; repeat.
+ * mhdgb_halo_bytes   bytes of face f's halo: 4-byte elements for a mixed handle prepared for fused
+ *                    steps, 8-byte elements otherwise (the FP64 forms, and the stage path, which
+ *                    works on FP64 primitives);
+ * mhdgb_halo_pack    copies the 2 interior layers next to face f into buf (device memory, or mapped
+ *                    page-locked host memory); mhdgb_halo_unpack copies buf into the 2 ghost layers
+ *                    beyond face f.  Both act on the primitives the next fused step reads (or, if
+ *                    the handle is not prepared for fused steps, on the stage path's) and return
+ *                    once the copy is done;
+ * mhdgb_get_reduction / mhdgb_set_reduction  read / replace the pending reduction of the next fused
+ *                    step: the minimum over the block of the cell CFL time (dt = cfl * dtmin) and
+ *                    the maximum signal speed (c_h).  The stage path reduces with
+ *                    mhdgb_control_timestep / mhdgb_evaluate_ch and takes the global values through
+ *                    mhdgb_set_dt / mhdgb_set_chg. */
+size_t mhdgb_halo_bytes(const mhdgb_solver* h, int face);
+int mhdgb_halo_pack(mhdgb_solver* h, int face, void* buf);
+int mhdgb_halo_unpack(mhdgb_solver* h, int face, const void* buf);
+int mhdgb_get_reduction(mhdgb_solver* h, double* dtmin, double* chmax);
+int mhdgb_set_reduction(mhdgb_solver* h, double dtmin, double chmax);
+
+/* A domain: one grid cut into ntiles[0] x ntiles[1] x ntiles[2] blocks inside one process.
+ * Block b has coordinates (b / (nt1*nt2), (b / nt2) % nt1, b % nt2), the row-major rank order of
+ * MPI_Cart_create; along each axis the first (n % nt) blocks take one cell more than the others.
+ * Each block takes its cell faces from the whole grid (so results do not depend on the split:
+ * a decomposed run equals the single-grid run bit for bit; the reference's ranks instead compute
+ * their own faces from their extent, main.cpp:35-64, which can differ in the last bit).
+ * Block b belongs to group b % ngroups, run on devices[b % ngroups] (ngroups = 0: one group on
+ * cfg->device).  Each step, each group advances its blocks in one persistent launch of the fused
+ * kernel; then, after every group's launch, each group copies the halos of its blocks' exchanged
+ * faces straight from the neighbouring blocks' primitives (over NVLink when the neighbour is on
+ * another GPU; peer access is enabled at creation) and reduces dt and c_h over all blocks.  Nothing
+ * returns to the host between steps; a one-group domain captures its steps in CUDA graphs.
+ * Requirements: spacing_quirk = 0, at least 2 cells per block and axis, boundary kinds 1..3.
+ * Whole-grid arrays are in the reference layout with the whole grid's extents. */
+typedef struct mhdgb_domain mhdgb_domain;
+int mhdgb_domain_create(const mhdgb_config* cfg, const int ntiles[3], int ngroups, const int* devices,
+                        mhdgb_domain** out);
+int mhdgb_domain_destroy(mhdgb_domain* d);
+const char* mhdgb_domain_last_error(const mhdgb_domain* d);
+int mhdgb_domain_blocks(const mhdgb_domain* d);
+/* Block b's handle (owned by the domain) and its first interior cell / extent in the whole grid. */
+int mhdgb_domain_block(mhdgb_domain* d, int b, mhdgb_solver** h, int offset[3], int extent[3]);
+int mhdgb_domain_upload_cons(mhdgb_domain* d, const double* U);
+/* Writes the interior cells of the whole-grid array U; its ghost cells are left as they are. */
+int mhdgb_domain_download_cons(mhdgb_domain* d, double* U);
+/* The KH state of mhdgb_init_kh on the whole grid (the noise of a cell depends on its whole-grid
+ * index, not on the split). */
+int mhdgb_domain_init_kh(mhdgb_domain* d, unsigned long long seed, double vshear, double width, double bx,
+                         double amp, double sig, double noise);
+int mhdgb_domain_prepare(mhdgb_domain* d);
+int mhdgb_domain_step(mhdgb_domain* d, int nsteps);
+/* Waits for the steps; the report is block 0's (every block has the same step, time, dt and c_h)
+ * with the status bits of all blocks. */
+int mhdgb_domain_sync(mhdgb_domain* d, mhdgb_report* report);
+int mhdgb_domain_set_stop(mhdgb_domain* d, double tmax, long long max_steps);
+int mhdgb_domain_time_steps(mhdgb_domain* d, int nsteps, double* ms);
+/* KH diagnostic of the whole grid (blocks' volume-weighted sums recombined; equal to the
+ * single-grid diagnostic up to the order of the sums). */
+int mhdgb_domain_diag(mhdgb_domain* d, double out[3]);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,7 @@ _lib = None
 MHDGB_FP64, MHDGB_FP64_EXACT, MHDGB_MIXED = 0, 1, 2
 PRECISIONS = {"fp64": MHDGB_FP64, "fp64_exact": MHDGB_FP64_EXACT, "mixed": MHDGB_MIXED}
 RIEMANN = {"hlld": 0, "hlle": 1, "hllc": 2}
+BC_EXCHANGE = 4  # a face shared with another block of a decomposed grid
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "non-positive rho/p",
           -5: "device wait timed out", -6: "call out of order", -7: "device allocation failed",
           -8: "grid too large for the fixed scratch", -9: "file output failed"}
@@ -86,6 +87,8 @@ SIGNATURES = {
     "mhdgb_variant_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int)]),
     "mhdgb_variant_name": (C.c_char_p, [_vp, C.c_int]),
+    "mhdgb_work_layout": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]),
     "mhdgb_select_variant": (C.c_int, [_vp, C.c_int]),
     "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
     "mhdgb_measure_fp64_rate": (C.c_int, [C.c_int, _dp]),
@@ -94,6 +97,8 @@ SIGNATURES = {
     "mhdgb_diag": (C.c_int, [_vp, _dp]),
     "mhdgb_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double]),
+    "mhdgb_init_kh_block": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_ulonglong, C.c_double,
+                                      C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]),
     "mhdgb_ensemble_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(_vp)]),
     "mhdgb_ensemble_destroy": (C.c_int, [_vp]),
     "mhdgb_ensemble_last_error": (C.c_char_p, [_vp]),
@@ -108,6 +113,27 @@ SIGNATURES = {
     "mhdgb_ensemble_select_variant": (C.c_int, [_vp, C.c_int]),
     "mhdgb_ensemble_variant": (C.c_int, [_vp]),
     "mhdgb_ensemble_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
+    "mhdgb_halo_bytes": (C.c_size_t, [_vp, C.c_int]),
+    "mhdgb_halo_pack": (C.c_int, [_vp, C.c_int, _vp]),
+    "mhdgb_halo_unpack": (C.c_int, [_vp, C.c_int, _vp]),
+    "mhdgb_get_reduction": (C.c_int, [_vp, _dp, _dp]),
+    "mhdgb_set_reduction": (C.c_int, [_vp, C.c_double, C.c_double]),
+    "mhdgb_domain_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int),
+                                      C.POINTER(_vp)]),
+    "mhdgb_domain_destroy": (C.c_int, [_vp]),
+    "mhdgb_domain_last_error": (C.c_char_p, [_vp]),
+    "mhdgb_domain_blocks": (C.c_int, [_vp]),
+    "mhdgb_domain_block": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mhdgb_domain_upload_cons": (C.c_int, [_vp, _dp]),
+    "mhdgb_domain_download_cons": (C.c_int, [_vp, _dp]),
+    "mhdgb_domain_init_kh": (C.c_int, [_vp, C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_double]),
+    "mhdgb_domain_prepare": (C.c_int, [_vp]),
+    "mhdgb_domain_step": (C.c_int, [_vp, C.c_int]),
+    "mhdgb_domain_sync": (C.c_int, [_vp, C.POINTER(Report)]),
+    "mhdgb_domain_set_stop": (C.c_int, [_vp, C.c_double, C.c_longlong]),
+    "mhdgb_domain_time_steps": (C.c_int, [_vp, C.c_int, _dp]),
+    "mhdgb_domain_diag": (C.c_int, [_vp, _dp]),
 }
 
 

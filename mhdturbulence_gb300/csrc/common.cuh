@@ -12,6 +12,11 @@ namespace mhdgb {
 
 constexpr int NGH = 2;  // ghost layers, src_cpp_kokkos_host/config.hpp:56
 
+// Boundary kind of a face shared with a neighbouring block of a decomposed grid: its ghost layers
+// are copied from the neighbour (the MPI branch of SendRecvBoundary, boundary.cpp:222-318), so no
+// local fill writes them.  Kinds 1..3 are the reference's (config.hpp:29-31).
+constexpr int BC_EXCHANGE = 4;
+
 // Device arrays use the reference FieldArray layout (src_cpp_kokkos_host/mhd.hpp:237-238,
 // View(n1,nv,n2,n3) LayoutLeft: i fastest, then variable, then j, then k) with the i extent
 // padded from itot = nx+2*ngh+1 to a pitch `ip` that makes every row 64-byte aligned (TMA needs

@@ -8,6 +8,8 @@ namespace mhdgb {
 
 enum FusedKind { FUSED_FP64_EXACT = 0, FUSED_FP64 = 1, FUSED_MIXED = 2 };
 
+constexpr int MAX_ZCHUNKS = 64;  // z chunks per tile column
+
 struct FusedShape {
   int tx, ty;          // columns of a tile
   size_t smem;         // dynamic shared memory per CTA
@@ -28,7 +30,10 @@ struct FusedArgs {
   int bc[6];
   int quirk;                           // y/z inverse spacing taken at index i (mhd.cpp:1435-1436)
   int riemann;                         // RIEMANN_HLLD / _HLLE / _HLLC
-  int ntx, nty, nkc, kc;               // tiles in x, y; chunks in z; planes per chunk
+  int ntx, nty, nkc;                   // tiles in x, y; chunks in z
+  // chunk c of every tile column covers planes [kst[c], kst[c+1]) (interior index); the work queue
+  // takes all tiles of chunk 0 first, so chunks that shrink with c even out the CTAs' finish times
+  int kst[MAX_ZCHUNKS + 1];
   Ctrl* ctrl;
   // End-to-end steps: the caller's host array of U (reference layout, itot x jtot x ktot, reached
   // over the host link), written by the step's cell updates besides U; null otherwise.

@@ -106,7 +106,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
     const int item = gitem - desc[inst].item_begin;
     const int bxi = item % a.ntx, byi = (item / a.ntx) % a.nty, bki = item / (a.ntx * a.nty);
     const int i0 = bxi * TX, j0 = byi * TY;
-    const int kb = bki * a.kc, ke = min(kb + a.kc, L.nz);
+    const int kb = a.kst[bki], ke = a.kst[bki + 1];
     const int cx = min(TX, L.nx - i0), cy = min(TY, L.ny - j0);
     const bool own = oj < TY && oi < cx && oj < cy;
     const int ii = i0 + oi, jj = j0 + oj;

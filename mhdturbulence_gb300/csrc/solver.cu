@@ -9,6 +9,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <cmath>
 #include <cstdio>
@@ -157,6 +158,57 @@ uint64_t splitmix64(uint64_t x) {
   return z ^ (z >> 31);
 }
 
+struct KhParams {
+  unsigned long long seed;
+  double vshear, width, bx, amp, sig, noise;
+};
+
+// Kelvin-Helmholtz initial state (the set-up of mhdturbulence_gb300/ic.py.kh_prim) on the device,
+// for the interior cells of a block whose first cell is cell (i0, j0, k0) of a gnx x gny x ... grid
+// (the noise of a cell is a counter hash of its whole-grid index, so it does not depend on the
+// split); xa / ya are the block's cell faces.  Ghost cells are left as they are.
+__global__ void k_init_kh(double* __restrict__ U, Layout L, const double* __restrict__ xa,
+                          const double* __restrict__ ya, int gnx, int gny, int i0, int j0, int k0, uint64_t key,
+                          double gam, double vshear, double width, double bx, double amp, double sig, double noise) {
+  const long long n = (long long)L.nx * L.ny * L.nz;
+  const double pi = 3.14159265358979323846;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
+    const double x = 0.5 * (xa[i + NGH + 1] + xa[i + NGH]);
+    const double y = 0.5 * (ya[j + NGH + 1] + ya[j + NGH]);
+    const uint64_t idx = ((uint64_t)(k + k0) * gny + (uint64_t)(j + j0)) * gnx + (uint64_t)(i + i0);
+    uint64_t z = (idx ^ key) + 0x9E3779B97F4A7C15ull;  // splitmix64
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    const double th = tanh(y / width);
+    const double rho = 1.0, p = 1.0;
+    const double vx = vshear * th;
+    const double ys = y / sig;
+    const double vy = amp * sin(2.0 * pi * x) * exp(-(ys * ys)) + noise * (2.0 * u - 1.0);
+    const double X = 0.5 * (1.0 + th);
+    const double e = p / (rho * (gam - 1.0));
+    const double ekin = 0.5 * rho * (vx * vx + vy * vy);
+    const double emag = 0.5 * (bx * bx);
+    const size_t c = L.at(NCONS, 0, k + NGH, j + NGH, i + NGH), fs = (size_t)L.ip;
+    U[c + mden * fs] = rho;
+    U[c + mrv1 * fs] = rho * vx;
+    U[c + mrv2 * fs] = rho * vy;
+    U[c + mrv3 * fs] = 0.0;
+    U[c + meto * fs] = rho * e + ekin + emag;
+    U[c + mbm1 * fs] = bx;
+    U[c + mbm2 * fs] = 0.0;
+    U[c + mbm3 * fs] = 0.0;
+    U[c + mbps * fs] = 0.0;
+    U[c + mst * fs] = rho * X;
+  }
+}
+
+uint64_t kh_key(unsigned long long seed) {
+  return splitmix64((uint64_t)seed * 0xD1B54A32D192ED03ull + 0ull * 0x8CB92BA72F3D8DD7ull);
+}
+
 }  // namespace
 
 struct mhdgb_solver {
@@ -175,6 +227,7 @@ struct mhdgb_solver {
   double *xinv = nullptr, *yinv = nullptr, *zinv = nullptr, *dxs = nullptr, *dys = nullptr, *dzs = nullptr;
   float *xinvf = nullptr, *yinvf = nullptr, *zinvf = nullptr, *dxsf = nullptr, *dysf = nullptr, *dzsf = nullptr;
   double* scal = nullptr;   // [0] dt, [1] chg of the stage path, [2..4] diagnostic, [8..] diag planes
+  double* faces = nullptr;  // x1a (itot) then x2a (jtot): the cell faces the KH initial state needs
   RedSlot* sslot = nullptr; // stage-path reduction slot
   Ctrl* ctrl = nullptr;
   size_t bytes = 0;
@@ -184,7 +237,8 @@ struct mhdgb_solver {
   const FusedVariant* vars = nullptr;  // compiled HLLD tile shapes of this precision; vars[nvars] is
   int nvars = 0, vidx = 0;             // the run-time solver kernel; vidx: the kernel in use
   int hlld_vidx = 0;                   // the HLLD variant to return to from HLLE/HLLC
-  int grid = 0, ntx = 0, nty = 0, nkc = 0, kc = 0;
+  int grid = 0, ntx = 0, nty = 0, nkc = 0;
+  std::vector<int> kst;      // z chunk boundaries (FusedArgs::kst)
   long long cur_step = 0;    // device step count as of the last sync (selects the current P)
   bool have_state = false;   // U uploaded
   bool prepared = false;     // fused buffers consistent with U
@@ -299,6 +353,8 @@ int upload_grid(mhdgb_solver* h) {
   CK(h, cudaMemcpy(h->dxsf, sx.data(), bf, cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->dysf, sy.data(), bf, cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->dzsf, sz.data(), bf, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->faces, h->x1a.data(), h->L.itot * sizeof(double), cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->faces + h->L.itot, h->x2a.data(), h->L.jtot * sizeof(double), cudaMemcpyHostToDevice));
   return MHDGB_OK;
 }
 
@@ -412,6 +468,14 @@ int ensure_p64(mhdgb_solver* h) {
   if (h->p64_valid) return MHDGB_OK;
   if (!h->have_state) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
   double* P = h->P64[cur_index(h)];
+  if (h->prepared && h->kind != FUSED_MIXED) {
+    // P64[cur] is the fused step's own recovery of U: recovering it again with the stage kernels'
+    // rounding could change its last bits under the running fused steps; only the ghost layers
+    // still need the reference's fill
+    CK(h, launch_ghost_fill(P, h->L, h->cfg.bc, h->pack, h->stream));
+    h->p64_valid = true;
+    return MHDGB_OK;
+  }
   CK(h, launch_update_prim(h->U, P, h->L, h->cfg.gam, h->stream));
   CK(h, launch_ghost_fill(P, h->L, h->cfg.bc, h->pack, h->stream));
   h->p64_valid = true;
@@ -440,7 +504,8 @@ FusedArgs fused_args(mhdgb_solver* h) {
   for (int q = 0; q < 6; q++) a.bc[q] = h->cfg.bc[q];
   a.quirk = h->cfg.spacing_quirk;
   a.riemann = h->riemann;
-  a.ntx = h->ntx; a.nty = h->nty; a.nkc = h->nkc; a.kc = h->kc;
+  a.ntx = h->ntx; a.nty = h->nty; a.nkc = h->nkc;
+  for (int c = 0; c <= h->nkc && c < (int)h->kst.size(); c++) a.kst[c] = h->kst[c];
   a.ctrl = h->ctrl;
   return a;
 }
@@ -472,10 +537,75 @@ int launch_one(mhdgb_solver* h) {
   return MHDGB_OK;
 }
 
+// Relative cost of one plane of a cx x cy tile: its face and slope work against a full tile's, plus
+// a fixed part (barriers, loads).  Only the ratios matter.
+double tile_plane_cost(int cx, int cy, int tx, int ty) {
+  auto warps = [](int n) { return (double)((n + 31) / 32); };
+  const double f = (double)(cy * (cx + 1) + (cy + 1) * cx + cy * cx), ff = (double)(ty * (tx + 1) + (ty + 1) * tx + ty * tx);
+  const double sl = warps(cy * (cx + 2)) + warps((cy + 2) * cx) + warps(cy * cx);
+  const double sf = warps(ty * (tx + 2)) + warps((ty + 2) * tx) + warps(ty * tx);
+  return 0.1 + 0.9 * (0.75 * f / ff + 0.25 * sl / sf);
+}
+
+// Finish time of the slowest of `grid` CTAs that take the work items in queue order (chunk-major,
+// then tile rows, then tiles), each CTA the next item when it finishes its last.  A chunk's start
+// costs about kOverheadPlanes planes more (prologue loads, the extra z faces of its first plane).
+double simulate_queue(const std::vector<double>& tile_cost, const std::vector<int>& chunks, int grid) {
+  constexpr double kOverheadPlanes = 0.6;
+  std::vector<double> heap(grid, 0.0);  // min-heap of CTA finish times
+  auto cmp = [](double a, double b) { return a > b; };
+  for (int c : chunks)
+    for (double tc : tile_cost) {
+      std::pop_heap(heap.begin(), heap.end(), cmp);
+      heap.back() += tc * (c + kOverheadPlanes);
+      std::push_heap(heap.begin(), heap.end(), cmp);
+    }
+  return *std::max_element(heap.begin(), heap.end());
+}
+
+// z chunks of a grid for a persistent launch of `grid` CTAs: among uniform chunkings and chunkings
+// whose sizes shrink (each chunk about remaining * tiles / (K * grid) planes, so the queue ends on
+// small items that fill the CTAs' last gaps), the one with the earliest simulated finish.
+std::vector<int> choose_chunks(const Layout& L, int tx, int ty, int ntx, int nty, int grid) {
+  std::vector<double> cost;
+  for (int by = 0; by < nty; by++)
+    for (int bx = 0; bx < ntx; bx++)
+      cost.push_back(tile_plane_cost(std::min(tx, L.nx - bx * tx), std::min(ty, L.ny - by * ty), tx, ty));
+  const int tiles = ntx * nty, nz = L.nz;
+  std::vector<std::vector<int>> cand;
+  for (int n = 1; n <= std::min(nz, 32); n++) {
+    const int kc = (nz + n - 1) / n;
+    std::vector<int> c;
+    for (int k = 0; k < nz; k += kc) c.push_back(std::min(kc, nz - k));
+    if ((int)c.size() <= MAX_ZCHUNKS) cand.push_back(c);
+  }
+  const double Ks[] = {1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0};
+  for (double K : Ks)
+    for (int minc : {2, 4, 8}) {
+      std::vector<int> c;
+      int rem = nz;
+      while (rem > 0) {
+        int s = std::max(minc, (int)std::ceil(rem * (double)tiles / (K * grid)));
+        s = std::min(s, rem);
+        if (rem - s < minc) s = rem;
+        c.push_back(s);
+        rem -= s;
+      }
+      if ((int)c.size() <= MAX_ZCHUNKS) cand.push_back(c);
+    }
+  double best = 1e300;
+  std::vector<int> pick{nz};
+  for (const auto& c : cand) {
+    const double t = simulate_queue(cost, c, grid);
+    if (t < best * (1.0 - 1e-9)) { best = t; pick = c; }
+  }
+  return pick;
+}
+
 // Make variant idx the one in use: kernel attribute, grid, work decomposition, tensor maps.
-// kc_fixed > 0 sets the planes per work item directly (ensembles keep items of similar size);
-// otherwise the z chunks give about items_per_cta work items per CTA.
-int use_variant(mhdgb_solver* h, int idx, int items_per_cta, int kc_fixed = 0) {
+// kc_fixed > 0 cuts z into chunks of kc_fixed planes (ensembles keep items of similar size across
+// their grids); otherwise the chunking with the best simulated balance is taken (choose_chunks).
+int use_variant(mhdgb_solver* h, int idx, int kc_fixed = 0) {
   if (idx < 0 || idx > h->nvars) return fail(h, MHDGB_ERR_ARG, "no such variant");
   const FusedVariant& v = h->vars[idx];
   CK(h, v.prepare());
@@ -488,12 +618,16 @@ int use_variant(mhdgb_solver* h, int idx, int items_per_cta, int kc_fixed = 0) {
   const Layout& L = h->L;
   h->ntx = (L.nx + h->shape.tx - 1) / h->shape.tx;
   h->nty = (L.ny + h->shape.ty - 1) / h->shape.ty;
-  // z chunks: about items_per_cta work items per CTA for load balance, chunks of >= 4 planes
-  const int tiles = h->ntx * h->nty;
-  int nkc = (items_per_cta * h->grid + tiles - 1) / tiles;
-  nkc = std::max(1, std::min(nkc, std::max(1, L.nz / 4)));
-  h->kc = kc_fixed > 0 ? std::min(kc_fixed, L.nz) : (L.nz + nkc - 1) / nkc;
-  h->nkc = (L.nz + h->kc - 1) / h->kc;
+  std::vector<int> chunks;
+  if (kc_fixed > 0) {
+    const int kc = std::max(std::min(kc_fixed, L.nz), (L.nz + MAX_ZCHUNKS - 1) / MAX_ZCHUNKS);
+    for (int k = 0; k < L.nz; k += kc) chunks.push_back(std::min(kc, L.nz - k));
+  } else {
+    chunks = choose_chunks(L, h->shape.tx, h->shape.ty, h->ntx, h->nty, h->grid);
+  }
+  h->nkc = (int)chunks.size();
+  h->kst.assign(1, 0);
+  for (int c : chunks) h->kst.push_back(h->kst.back() + c);
   void* pbase[2] = {h->kind == FUSED_MIXED ? (void*)h->P32[0] : (void*)h->P64[0],
                     h->kind == FUSED_MIXED ? (void*)h->P32[1] : (void*)h->P64[1]};
   int rc;
@@ -601,7 +735,7 @@ int create_impl(const mhdgb_config* cfg, cudaStream_t shared, mhdgb_solver** out
   if (cfg->nx < 2 || cfg->ny < 2 || cfg->nz < 2) return MHDGB_ERR_ARG;
   if (!(cfg->gam > 1.0) || !(cfg->cfl > 0.0)) return MHDGB_ERR_ARG;
   for (int q = 0; q < 6; q++)
-    if (cfg->bc[q] < 1 || cfg->bc[q] > 3) return MHDGB_ERR_ARG;
+    if (cfg->bc[q] < MHDGB_BC_PERIODIC || cfg->bc[q] > MHDGB_BC_EXCHANGE) return MHDGB_ERR_ARG;
   if (cfg->precision < MHDGB_FP64 || cfg->precision > MHDGB_MIXED) return MHDGB_ERR_ARG;
   if (cfg->spacing_quirk && (cfg->nx > cfg->ny || cfg->nx > cfg->nz)) return MHDGB_ERR_ARG;
   mhdgb_solver* h = new mhdgb_solver();
@@ -640,6 +774,7 @@ int create_impl(const mhdgb_config* cfg, cudaStream_t shared, mhdgb_solver** out
        dalloc(h, &h->zinvf, nmax) == cudaSuccess && dalloc(h, &h->dxsf, nmax) == cudaSuccess &&
        dalloc(h, &h->dysf, nmax) == cudaSuccess && dalloc(h, &h->dzsf, nmax) == cudaSuccess;
   ok = ok && dalloc(h, &h->scal, 8 + 3 * (size_t)L.nz) == cudaSuccess;
+  ok = ok && dalloc(h, &h->faces, (size_t)L.itot + L.jtot) == cudaSuccess;
   ok = ok && dalloc(h, &h->sslot, 1) == cudaSuccess && dalloc(h, &h->ctrl, 1) == cudaSuccess;
   if (!ok) return cleanup(MHDGB_ERR_NOMEM);
   h->x1a = face_axis(cfg->nx, cfg->x1min, cfg->x1max);
@@ -653,7 +788,7 @@ int create_impl(const mhdgb_config* cfg, cudaStream_t shared, mhdgb_solver** out
     auto& m = tune_cache();
     auto it = m.find(std::make_tuple((int)h->kind, L.nx, L.ny, L.nz));
     if (it != m.end() && it->second < h->nvars) idx = it->second;
-    if ((rc = use_variant(h, idx, 4)) && (idx == 0 || (rc = use_variant(h, 0, 4)))) return cleanup(rc);
+    if ((rc = use_variant(h, idx)) && (idx == 0 || (rc = use_variant(h, 0)))) return cleanup(rc);
   }
   k_ctrl_reset<<<1, 1, 0, h->stream>>>(h->ctrl, 0);
   k_ctrl_set_stop<<<1, 1, 0, h->stream>>>(h->ctrl, 1.0e300, ~0ull);
@@ -677,7 +812,7 @@ int mhdgb_destroy(mhdgb_solver* h) {
   destroy_graph(h);
   void* ptrs[] = {h->U, h->P64[0], h->P64[1], h->P32[0], h->P32[1], h->F[0], h->F[1], h->F[2], h->pack,
                   h->xinv, h->yinv, h->zinv, h->dxs, h->dys, h->dzs, h->xinvf, h->yinvf, h->zinvf,
-                  h->dxsf, h->dysf, h->dzsf, h->scal, h->sslot, h->ctrl, h->d_desc, h->d_lc, h->stage,
+                  h->dxsf, h->dysf, h->dzsf, h->scal, h->faces, h->sslot, h->ctrl, h->d_desc, h->d_lc, h->stage,
                   h->d_snap};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -712,7 +847,7 @@ int mhdgb_set_physics(mhdgb_solver* h, double gam, double cfl, const int* bc) {
   if (!h || !(gam > 1.0) || !(cfl > 0.0)) return MHDGB_ERR_ARG;
   if (bc)
     for (int q = 0; q < 6; q++)
-      if (bc[q] < 1 || bc[q] > 3) return MHDGB_ERR_ARG;
+      if (bc[q] < MHDGB_BC_PERIODIC || bc[q] > MHDGB_BC_EXCHANGE) return MHDGB_ERR_ARG;
   int rc = set_device(h);
   if (rc || (rc = settle(h))) return rc;
   const bool same = h->cfg.gam == gam && h->cfg.cfl == cfl &&
@@ -735,7 +870,7 @@ int mhdgb_set_riemann(mhdgb_solver* h, int solver) {
   h->riemann = solver;
   // HLLD runs on the tuned HLLD variants, HLLE/HLLC on the run-time solver kernel
   const int want = solver == MHDGB_RIEMANN_HLLD ? h->hlld_vidx : h->nvars;
-  if (want != h->vidx) return use_variant(h, want, 4);
+  if (want != h->vidx) return use_variant(h, want);
   destroy_graph(h);
   return upload_desc(h);
 }
@@ -1234,6 +1369,16 @@ int mhdgb_variant_info(const mhdgb_solver* h, int idx, int* tx, int* ty, int* th
   return MHDGB_OK;
 }
 
+int mhdgb_work_layout(const mhdgb_solver* h, int* ntx, int* nty, int* nchunks, int* kstart) {
+  if (!h) return MHDGB_ERR_ARG;
+  if (ntx) *ntx = h->ntx;
+  if (nty) *nty = h->nty;
+  if (nchunks) *nchunks = h->nkc;
+  if (kstart)
+    for (size_t c = 0; c < h->kst.size(); c++) kstart[c] = h->kst[c];
+  return MHDGB_OK;
+}
+
 const char* mhdgb_variant_name(const mhdgb_solver* h, int idx) {
   if (!h) return nullptr;
   if (idx == -1) idx = h->vidx;
@@ -1250,7 +1395,7 @@ int mhdgb_select_variant(mhdgb_solver* h, int idx) {
     return MHDGB_OK;
   }
   const bool was_prepared = h->prepared;
-  if ((rc = use_variant(h, idx, 4))) return rc;
+  if ((rc = use_variant(h, idx))) return rc;
   h->prepared = was_prepared;  // the P buffers and reduction slots do not depend on the tile shape
   return MHDGB_OK;
 }
@@ -1285,12 +1430,12 @@ int mhdgb_autotune(mhdgb_solver* h, int steps, int* best) {
   double best_ms = 1e300;
   int bidx = h->vidx;
   for (int v = 0; v < h->nvars; v++) {
-    if ((rc = use_variant(h, v, 4)) || (rc = restore())) return rc;
+    if ((rc = use_variant(h, v)) || (rc = restore())) return rc;
     double ms = 0.0;
     if ((rc = mhdgb_time_steps(h, 2, &ms)) || (rc = mhdgb_time_steps(h, steps, &ms))) return rc;
     if (ms < best_ms) { best_ms = ms; bidx = v; }
   }
-  if ((rc = use_variant(h, bidx, 4)) || (rc = restore())) return rc;
+  if ((rc = use_variant(h, bidx)) || (rc = restore())) return rc;
   tune_cache_store((int)h->kind, h->L, bidx);
   if (best) *best = bidx;
   return MHDGB_OK;
@@ -1304,6 +1449,8 @@ int mhdgb_diag(mhdgb_solver* h, double out[3]) {
   double* planes = h->scal + 8;
   if (h->kind == FUSED_MIXED && h->prepared) {
     k_diag_planes<float><<<L.nz, 256, 0, h->stream>>>(h->P32[cur_index(h)], L, h->dxs, h->dys, h->dzs, planes);
+  } else if (h->prepared) {  // the fused step's FP64 primitives, read as they are
+    k_diag_planes<double><<<L.nz, 256, 0, h->stream>>>(h->P64[cur_index(h)], L, h->dxs, h->dys, h->dzs, planes);
   } else {
     if ((rc = ensure_p64(h))) return rc;
     k_diag_planes<double><<<L.nz, 256, 0, h->stream>>>(h->P64[cur_index(h)], L, h->dxs, h->dys, h->dzs, planes);
@@ -1316,42 +1463,45 @@ int mhdgb_diag(mhdgb_solver* h, double out[3]) {
   return MHDGB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// The KH state of cell block (i0, j0, k0) + (nx, ny, nz) of a gnx x gny x ... grid into h's U
+// (ghost cells zero).
+int init_kh_block(mhdgb_solver* h, int gnx, int gny, int i0, int j0, int k0, const KhParams& kp) {
+  int rc = set_device(h);
+  if (rc || (rc = settle(h))) return rc;
+  const Layout& L = h->L;
+  CK(h, cudaMemsetAsync(h->U, 0, L.count(NCONS) * sizeof(double), h->stream));
+  const long long n = (long long)L.nx * L.ny * L.nz;
+  const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, (long long)h->nsm * 16);
+  k_init_kh<<<g, 256, 0, h->stream>>>(h->U, L, h->faces, h->faces + L.itot, gnx, gny, i0, j0, k0, kh_key(kp.seed),
+                                      h->cfg.gam, kp.vshear, kp.width, kp.bx, kp.amp, kp.sig, kp.noise);
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->have_state = true;
+  h->prepared = false;
+  h->p64_valid = h->p_user;
+  return MHDGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int mhdgb_init_kh(mhdgb_solver* h, unsigned long long seed, double vshear, double width, double bx, double amp,
                   double sig, double noise) {
   if (!h) return MHDGB_ERR_ARG;
-  const Layout& L = h->L;
-  const int it = L.itot, jt = L.jtot;
-  std::vector<double> U((size_t)NCONS * it * jt * L.ktot, 0.0);
-  const double pi = std::acos(-1.0), gam = h->cfg.gam;
-  const uint64_t key = splitmix64((uint64_t)seed * 0xD1B54A32D192ED03ull + 0ull * 0x8CB92BA72F3D8DD7ull);
-  for (int k = 0; k < L.nz; k++)
-    for (int j = 0; j < L.ny; j++)
-      for (int i = 0; i < L.nx; i++) {
-        const double x = 0.5 * (h->x1a[i + NGH + 1] + h->x1a[i + NGH]);
-        const double y = 0.5 * (h->x2a[j + NGH + 1] + h->x2a[j + NGH]);
-        const uint64_t idx = ((uint64_t)k * L.ny + j) * L.nx + i;
-        const double u = (double)(splitmix64(idx ^ key) >> 11) * (1.0 / 9007199254740992.0);
-        const double th = std::tanh(y / width);
-        const double rho = 1.0, p = 1.0;
-        const double vx = vshear * th;
-        const double vy = amp * std::sin(2.0 * pi * x) * std::exp(-(y / sig) * (y / sig)) + noise * (2.0 * u - 1.0);
-        const double vz = 0.0, by = 0.0, bz = 0.0, X = 0.5 * (1.0 + th);
-        const double e = p / (rho * (gam - 1.0));
-        const double ekin = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
-        const double emag = 0.5 * (bx * bx + by * by + bz * bz);
-        auto at = [&](int m) { return (size_t)(i + NGH) + (size_t)it * (m + (size_t)NCONS * ((j + NGH) + (size_t)jt * (k + NGH))); };
-        U[at(mden)] = rho;
-        U[at(mrv1)] = rho * vx;
-        U[at(mrv2)] = rho * vy;
-        U[at(mrv3)] = rho * vz;
-        U[at(meto)] = rho * e + ekin + emag;
-        U[at(mbm1)] = bx;
-        U[at(mbm2)] = by;
-        U[at(mbm3)] = bz;
-        U[at(mbps)] = 0.0;
-        U[at(mst)] = rho * X;
-      }
-  return mhdgb_upload_cons(h, U.data());
+  return init_kh_block(h, h->L.nx, h->L.ny, 0, 0, 0, KhParams{seed, vshear, width, bx, amp, sig, noise});
+}
+
+int mhdgb_init_kh_block(mhdgb_solver* h, const int whole[3], const int offset[3], unsigned long long seed,
+                        double vshear, double width, double bx, double amp, double sig, double noise) {
+  if (!h || !whole || !offset) return MHDGB_ERR_ARG;
+  if (offset[0] < 0 || offset[1] < 0 || offset[2] < 0 || offset[0] + h->L.nx > whole[0] ||
+      offset[1] + h->L.ny > whole[1] || offset[2] + h->L.nz > whole[2])
+    return fail(h, MHDGB_ERR_ARG, "block does not lie inside the whole grid");
+  return init_kh_block(h, whole[0], whole[1], offset[0], offset[1], offset[2],
+                       KhParams{seed, vshear, width, bx, amp, sig, noise});
 }
 
 int mhdgb_selftest_fused_abort(int device, int precision, double* seconds, unsigned* status, int* recovered) {
@@ -1462,7 +1612,7 @@ int ens_use_variant(mhdgb_ensemble* e, int idx) {
   int begin = 0;
   for (size_t i = 0; i < e->m.size(); i++) {
     const bool was = e->m[i]->prepared;
-    int rc = use_variant(e->m[i], eff, 4, e->kc);
+    int rc = use_variant(e->m[i], eff, e->kc);
     if (rc) return ens_member_rc(e, (int)i, rc);
     e->m[i]->prepared = was;
     d[i] = host_desc(e->m[i], begin);
@@ -1889,6 +2039,694 @@ int mhdgb_checkpoint_load(mhdgb_solver* h, const char* path) {
   h->prepared = false;
   h->p64_valid = false;
   h->p_user = false;
+  return MHDGB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Block decomposition.  The reference splits the grid over MPI ranks with MPI_Cart_create
+// (mpi_config.cpp:61-69), swaps 2-deep primitive halos with its neighbours inside SendRecvBoundary
+// (boundary.cpp:222-318, 430-475, 627-672) and reduces dt and c_h with MPI_MINLOC / MPI_MAXLOC
+// allreduces (mpi_config.cpp:83-99).  Here a block is an ordinary handle whose shared faces have
+// the kind MHDGB_BC_EXCHANGE (no local fill writes their ghosts).  Two ways to drive blocks:
+//   * per handle (one process per GPU, any transport): mhdgb_halo_pack / _unpack move a face's
+//     2-deep slab between the handle's primitives and a contiguous buffer, and
+//     mhdgb_get_reduction / _set_reduction read and replace the pending dt / c_h reduction;
+//   * a domain (one process, one or more GPUs): the blocks of each group advance in one persistent
+//     launch of the fused kernel, then one kernel per group copies every exchanged halo straight
+//     from the neighbouring block's primitives (a peer read over NVLink when the neighbour is on
+//     another GPU; no staging buffer), and one thread reduces dt and c_h over all blocks into the
+//     group's own control blocks.  Nothing leaves the devices between steps.
+// Only the interior transverse extent of a face is exchanged: the solver never reads the edge and
+// corner ghosts that the reference's full-extent buffers also carry.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+// The 2-deep box of face f (0..5 = x-in, x-out, y-in, y-out, z-in, z-out) in the reference index
+// space: the interior layers next to the face (ghost = false) or the ghost layers beyond it.
+struct FaceBox {
+  int lo[3], n[3];  // start and count along i, j, k
+};
+
+__host__ __device__ inline FaceBox face_box(const Layout& L, int face, bool ghost) {
+  FaceBox b{{NGH, NGH, NGH}, {L.nx, L.ny, L.nz}};
+  const int ax = face >> 1, hi = face & 1;
+  b.lo[ax] = ghost ? (hi ? NGH + b.n[ax] : 0) : (hi ? NGH + b.n[ax] - 2 : NGH);
+  b.n[ax] = 2;
+  return b;
+}
+
+__host__ __device__ inline long long box_count(const FaceBox& b) {
+  return (long long)NPRIM * b.n[0] * b.n[1] * b.n[2];
+}
+
+// Element e of a box (i fastest, then j, k, variable) as an offset into a primitive array.
+__host__ __device__ inline size_t box_at(const Layout& L, const FaceBox& b, long long e) {
+  const int i = (int)(e % b.n[0]);
+  const int j = (int)((e / b.n[0]) % b.n[1]);
+  const int k = (int)((e / ((long long)b.n[0] * b.n[1])) % b.n[2]);
+  const int n = (int)(e / ((long long)b.n[0] * b.n[1] * b.n[2]));
+  return L.at(NPRIM, n, b.lo[2] + k, b.lo[1] + j, b.lo[0] + i);
+}
+
+// Face slab <-> contiguous buffer (box order).
+template <class R>
+__global__ void k_halo_copy(R* __restrict__ P, Layout L, FaceBox b, R* __restrict__ buf, int to_buf) {
+  const long long n = box_count(b);
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const size_t o = box_at(L, b, e);
+    if (to_buf) buf[e] = P[o];
+    else P[o] = buf[e];
+  }
+}
+
+// One exchanged face of a domain: the source block's interior slab goes to the destination block's
+// ghost layers, in the primitive buffer of the current step's parity.
+struct HaloXfer {
+  const void* src[2];
+  void* dst[2];
+  Layout Ls, Ld;
+  FaceBox bs, bd;
+  const Ctrl* ctrl;   // the destination's control block (its step selects the parity)
+  long long begin;    // first element of this transfer in the launch's element range
+};
+
+template <class R>
+__global__ void k_halo_exchange(const HaloXfer* __restrict__ x, int nx, long long total) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    int t = 0;
+    for (int lo = 0, hi = nx - 1; lo <= hi;) {
+      const int mid = (lo + hi) >> 1;
+      if (x[mid].begin <= e) { t = mid; lo = mid + 1; } else hi = mid - 1;
+    }
+    const HaloXfer& q = x[t];
+    const int par = (int)(q.ctrl->step & 1);
+    const long long r = e - q.begin;
+    static_cast<R*>(q.dst[par])[box_at(q.Ld, q.bd, r)] = static_cast<const R*>(q.src[par])[box_at(q.Ls, q.bs, r)];
+  }
+}
+
+// dt / c_h over all blocks of a domain, written into the pending slot of this group's blocks.  The
+// pending slot of a block is slot[step % 3]: the one its next fused step takes dt and c_h from.
+__global__ void k_domain_reduce(Ctrl* const* __restrict__ all, int nall, Ctrl* const* __restrict__ own, int nown) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long dtmin = DT_RESET, chmax = CH_RESET;
+  for (int q = 0; q < nall; q++) {
+    const Ctrl* c = all[q];
+    const RedSlot s = c->slot[c->step % 3];
+    dtmin = s.dtmin_bits < dtmin ? s.dtmin_bits : dtmin;
+    chmax = s.chmax_bits > chmax ? s.chmax_bits : chmax;
+  }
+  for (int q = 0; q < nown; q++) {
+    Ctrl* c = own[q];
+    c->slot[c->step % 3].dtmin_bits = dtmin;
+    c->slot[c->step % 3].chmax_bits = chmax;
+  }
+}
+
+__global__ void k_get_slot(const Ctrl* c, RedSlot* out) { *out = c->slot[c->step % 3]; }
+__global__ void k_set_slot(Ctrl* c, RedSlot v) { c->slot[c->step % 3] = v; }
+
+// The primitive array a halo call works on: the fused step's current buffer once the handle is
+// prepared for fused steps, else the stage path's FP64 primitives.
+int halo_target(mhdgb_solver* h, void** P, int* elem) {
+  int rc;
+  if ((rc = settle(h))) return rc;
+  if (h->prepared) {
+    const int c = cur_index(h);
+    *P = h->kind == FUSED_MIXED ? (void*)h->P32[c] : (void*)h->P64[c];
+    *elem = h->kind == FUSED_MIXED ? 4 : 8;
+    return MHDGB_OK;
+  }
+  if ((rc = ensure_p64(h))) return rc;
+  *P = h->P64[cur_index(h)];
+  *elem = 8;
+  return MHDGB_OK;
+}
+
+// The address a kernel reaches buf at: device (or managed) memory as it is, page-locked host
+// memory through its device mapping; null for pageable host memory, which no kernel can reach.
+void* kernel_view(void* buf) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, buf) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return buf;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
+int halo_copy(mhdgb_solver* h, int face, void* buf, int to_buf) {
+  if (!h || !buf || face < 0 || face > 5) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  void* P = nullptr;
+  int elem = 8;
+  if (rc || (rc = halo_target(h, &P, &elem))) return rc;
+  buf = kernel_view(buf);
+  if (!buf) return fail(h, MHDGB_ERR_ARG, "halo buffer is neither device memory nor page-locked host memory");
+  const FaceBox b = face_box(h->L, face, !to_buf);
+  const long long n = box_count(b);
+  const int bs = 256;
+  const unsigned g = (unsigned)std::min<long long>((n + bs - 1) / bs, (long long)h->nsm * 8);
+  if (elem == 4) k_halo_copy<float><<<g, bs, 0, h->stream>>>((float*)P, h->L, b, (float*)buf, to_buf);
+  else k_halo_copy<double><<<g, bs, 0, h->stream>>>((double*)P, h->L, b, (double*)buf, to_buf);
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (!to_buf) h->p_user = false;
+  return MHDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t mhdgb_halo_bytes(const mhdgb_solver* h, int face) {
+  if (!h || face < 0 || face > 5) return 0;
+  const size_t elem = (h->prepared && h->kind == FUSED_MIXED) ? 4 : 8;
+  return (size_t)box_count(face_box(h->L, face, false)) * elem;
+}
+
+int mhdgb_halo_pack(mhdgb_solver* h, int face, void* buf) { return halo_copy(h, face, buf, 1); }
+
+int mhdgb_halo_unpack(mhdgb_solver* h, int face, const void* buf) {
+  return halo_copy(h, face, const_cast<void*>(buf), 0);
+}
+
+int mhdgb_get_reduction(mhdgb_solver* h, double* dtmin, double* chmax) {
+  if (!h || !dtmin || !chmax) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->prepared) return fail(h, MHDGB_ERR_STATE, "no pending reduction: call mhdgb_prepare or step first");
+  RedSlot* d = h->sslot;  // the stage path's slot doubles as the transfer cell
+  k_get_slot<<<1, 1, 0, h->stream>>>(h->ctrl, d);
+  CK(h, cudaGetLastError());
+  RedSlot v;
+  CK(h, cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  *dtmin = bitsd(v.dtmin_bits);
+  *chmax = bitsd(v.chmax_bits);
+  return MHDGB_OK;
+}
+
+int mhdgb_set_reduction(mhdgb_solver* h, double dtmin, double chmax) {
+  if (!h || !(dtmin >= 0.0) || !(chmax >= 0.0)) return MHDGB_ERR_ARG;
+  int rc = set_device(h);
+  if (rc) return rc;
+  if (!h->prepared) return fail(h, MHDGB_ERR_STATE, "no pending reduction: call mhdgb_prepare or step first");
+  k_set_slot<<<1, 1, 0, h->stream>>>(h->ctrl, RedSlot{dbits(dtmin), dbits(chmax)});
+  CK(h, cudaGetLastError());
+  CK(h, cudaStreamSynchronize(h->stream));
+  return MHDGB_OK;
+}
+
+}  // extern "C"
+
+// A grid cut into blocks on one or more devices, advanced as one.
+struct mhdgb_domain {
+  mhdgb_config cfg{};                       // the whole grid
+  int nt[3] = {1, 1, 1};                    // blocks per axis
+  std::vector<double> x1a, x2a, x3a;        // the whole grid's faces
+  std::vector<mhdgb_ensemble*> groups;      // one persistent launch per group and step
+  std::vector<int> group_dev;
+  std::vector<mhdgb_solver*> blocks;        // block b at coords (b / (nt1*nt2), (b / nt2) % nt1, b % nt2)
+  std::vector<int> block_group;
+  std::vector<std::array<int, 3>> off, ext; // first interior cell (whole-grid index) and extent
+  struct Group {
+    HaloXfer* d_xfer = nullptr;
+    int nxfer = 0;
+    long long total = 0;
+    Ctrl** d_all = nullptr;
+    Ctrl** d_own = nullptr;
+    int nown = 0;
+    cudaEvent_t ev_step = nullptr, ev_halo = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+  };
+  std::vector<Group> g;
+  bool prepared = false;
+  std::string err;
+};
+
+namespace {
+
+int dfail(mhdgb_domain* d, int code, const std::string& msg) {
+  if (d) d->err = msg;
+  return code;
+}
+
+#define DCK(d, call)                                                                      \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return dfail((d), MHDGB_ERR_CUDA, std::string(#call) + ": " + \
+                                        cudaGetErrorString(e_));                          \
+  } while (0)
+
+// Cells of block c (of nt) along an axis of n cells: the first n % nt blocks take one more.
+void split_axis(int n, int nt, int c, int* off, int* len) {
+  const int base = n / nt, rem = n % nt;
+  *len = base + (c < rem ? 1 : 0);
+  *off = c * base + std::min(c, rem);
+}
+
+int block_of(const mhdgb_domain* d, int c0, int c1, int c2) { return (c0 * d->nt[1] + c1) * d->nt[2] + c2; }
+
+// Enqueue the halo copies and the reduction of group q on its stream.
+int domain_exchange(mhdgb_domain* d, int q) {
+  mhdgb_domain::Group& G = d->g[q];
+  mhdgb_ensemble* e = d->groups[q];
+  if (G.total > 0) {
+    const int bs = 256;
+    const unsigned grid = (unsigned)std::min<long long>((G.total + bs - 1) / bs, (long long)e->nsm * 8);
+    if (e->kind == FUSED_MIXED) k_halo_exchange<float><<<grid, bs, 0, e->stream>>>(G.d_xfer, G.nxfer, G.total);
+    else k_halo_exchange<double><<<grid, bs, 0, e->stream>>>(G.d_xfer, G.nxfer, G.total);
+    DCK(d, cudaGetLastError());
+  }
+  k_domain_reduce<<<1, 32, 0, e->stream>>>(G.d_all, (int)d->blocks.size(), G.d_own, G.nown);
+  DCK(d, cudaGetLastError());
+  return MHDGB_OK;
+}
+
+// One domain step: every group's launch, then (after all launches) every group's exchange.  With
+// one group everything is on one stream; with more, events order the groups' streams.
+int domain_step_once(mhdgb_domain* d) {
+  const int ng = (int)d->groups.size();
+  for (int q = 0; q < ng; q++) {
+    mhdgb_ensemble* e = d->groups[q];
+    DCK(d, cudaSetDevice(e->device));
+    if (ng > 1)
+      for (int r = 0; r < ng; r++)
+        if (r != q) DCK(d, cudaStreamWaitEvent(e->stream, d->g[r].ev_halo, 0));
+    int rc = ens_launch(e);
+    if (rc) return dfail(d, rc, e->err);
+    if (ng > 1) DCK(d, cudaEventRecord(d->g[q].ev_step, e->stream));
+  }
+  for (int q = 0; q < ng; q++) {
+    mhdgb_ensemble* e = d->groups[q];
+    DCK(d, cudaSetDevice(e->device));
+    if (ng > 1)
+      for (int r = 0; r < ng; r++)
+        if (r != q) DCK(d, cudaStreamWaitEvent(e->stream, d->g[r].ev_step, 0));
+    int rc = domain_exchange(d, q);
+    if (rc) return rc;
+    if (ng > 1) DCK(d, cudaEventRecord(d->g[q].ev_halo, e->stream));
+  }
+  return MHDGB_OK;
+}
+
+int domain_sync_streams(mhdgb_domain* d) {
+  for (auto* e : d->groups) {
+    DCK(d, cudaSetDevice(e->device));
+    DCK(d, cudaStreamSynchronize(e->stream));
+  }
+  return MHDGB_OK;
+}
+
+int domain_destroy_graphs(mhdgb_domain* d);
+
+// Recover every block's primitives from its U, then exchange the halos and reduce the first dt.
+// (A re-prepare may change a group's kernel, e.g. after mhdgb_set_riemann on a block: the captured
+// steps are dropped.)
+int domain_prepare(mhdgb_domain* d) {
+  domain_destroy_graphs(d);
+  for (auto* e : d->groups) {
+    DCK(d, cudaSetDevice(e->device));
+    int rc = ens_prepare_all(e, true);
+    if (rc) return dfail(d, rc, e->err);
+  }
+  const int ng = (int)d->groups.size();
+  for (int q = 0; q < ng; q++) {
+    mhdgb_ensemble* e = d->groups[q];
+    DCK(d, cudaSetDevice(e->device));
+    int rc = domain_exchange(d, q);
+    if (rc) return rc;
+    if (ng > 1) DCK(d, cudaEventRecord(d->g[q].ev_halo, e->stream));
+  }
+  int rc = domain_sync_streams(d);
+  if (rc) return rc;
+  d->prepared = true;
+  return MHDGB_OK;
+}
+
+int domain_destroy_graphs(mhdgb_domain* d) {
+  for (auto& G : d->g)
+    if (G.gexec) { cudaGraphExecDestroy(G.gexec); G.gexec = nullptr; }
+  return MHDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhdgb_domain_create(const mhdgb_config* cfg, const int ntiles[3], int ngroups, const int* devices,
+                        mhdgb_domain** out) {
+  if (!cfg || !ntiles || !out) return MHDGB_ERR_ARG;
+  *out = nullptr;
+  for (int a = 0; a < 3; a++)
+    if (ntiles[a] < 1) return MHDGB_ERR_ARG;
+  const int nb = ntiles[0] * ntiles[1] * ntiles[2];
+  if (cfg->nx / ntiles[0] < 2 || cfg->ny / ntiles[1] < 2 || cfg->nz / ntiles[2] < 2) return MHDGB_ERR_ARG;
+  for (int q = 0; q < 6; q++)
+    if (cfg->bc[q] < MHDGB_BC_PERIODIC || cfg->bc[q] > MHDGB_BC_OUTFLOW) return MHDGB_ERR_ARG;
+  if (cfg->spacing_quirk) return MHDGB_ERR_ARG;  // index-i spacings do not survive a split
+  if (ngroups < 0 || (ngroups > 0 && !devices) || ngroups > nb) return MHDGB_ERR_ARG;
+  if (ngroups == 0) ngroups = 1;
+  mhdgb_domain* d = new mhdgb_domain();
+  d->cfg = *cfg;
+  for (int a = 0; a < 3; a++) d->nt[a] = ntiles[a];
+  d->x1a = face_axis(cfg->nx, cfg->x1min, cfg->x1max);
+  d->x2a = face_axis(cfg->ny, cfg->x2min, cfg->x2max);
+  d->x3a = face_axis(cfg->nz, cfg->x3min, cfg->x3max);
+  const int n[3] = {cfg->nx, cfg->ny, cfg->nz};
+  // block configurations, grouped: block b goes to group b % ngroups
+  std::vector<std::vector<mhdgb_config>> gcfg(ngroups);
+  std::vector<std::vector<int>> gblocks(ngroups);
+  d->off.resize(nb);
+  d->ext.resize(nb);
+  d->block_group.resize(nb);
+  for (int b = 0; b < nb; b++) {
+    const int c[3] = {b / (ntiles[1] * ntiles[2]), (b / ntiles[2]) % ntiles[1], b % ntiles[2]};
+    mhdgb_config bc = *cfg;
+    int* dims[3] = {&bc.nx, &bc.ny, &bc.nz};
+    for (int a = 0; a < 3; a++) {
+      split_axis(n[a], ntiles[a], c[a], &d->off[b][a], dims[a]);
+      d->ext[b][a] = *dims[a];
+      // a face on the whole grid's boundary keeps its kind unless it wraps around to another block
+      // (periodic with more than one block along the axis); every inner face is exchanged
+      for (int side = 0; side < 2; side++) {
+        const bool edge = side == 0 ? c[a] == 0 : c[a] == ntiles[a] - 1;
+        const int f = 2 * a + side;
+        if (!edge || (cfg->bc[f] == MHDGB_BC_PERIODIC && ntiles[a] > 1)) bc.bc[f] = MHDGB_BC_EXCHANGE;
+      }
+    }
+    const int q = b % ngroups;
+    bc.device = devices ? devices[q] : cfg->device;
+    gcfg[q].push_back(bc);
+    gblocks[q].push_back(b);
+    d->block_group[b] = q;
+  }
+  d->blocks.assign(nb, nullptr);
+  d->g.resize(ngroups);
+  auto cleanup = [&](int code) { mhdgb_domain_destroy(d); return code; };
+  for (int q = 0; q < ngroups; q++) {
+    mhdgb_ensemble* e = nullptr;
+    int rc = mhdgb_ensemble_create((int)gcfg[q].size(), gcfg[q].data(), &e);
+    if (rc) return cleanup(rc);
+    d->groups.push_back(e);
+    d->group_dev.push_back(gcfg[q][0].device);
+    for (size_t i = 0; i < gblocks[q].size(); i++) d->blocks[gblocks[q][i]] = e->m[i];
+  }
+  // peer access between the groups' distinct devices (each group reads its neighbours' slabs)
+  for (int q = 0; q < ngroups; q++)
+    for (int r = 0; r < ngroups; r++) {
+      const int a = d->group_dev[q], b = d->group_dev[r];
+      if (a == b) continue;
+      int ok = 0;
+      if (cudaDeviceCanAccessPeer(&ok, a, b) != cudaSuccess || !ok) {
+        d->err = "devices " + std::to_string(a) + " and " + std::to_string(b) + " have no peer access";
+        return cleanup(MHDGB_ERR_ARG);
+      }
+      cudaSetDevice(a);
+      const cudaError_t pe = cudaDeviceEnablePeerAccess(b, 0);
+      if (pe != cudaSuccess && pe != cudaErrorPeerAccessAlreadyEnabled) return cleanup(MHDGB_ERR_CUDA);
+      cudaGetLastError();
+    }
+  // each block's faces are the whole grid's, sliced: results do not depend on the split
+  for (int b = 0; b < nb; b++) {
+    const auto& o = d->off[b];
+    int rc = mhdgb_set_grid(d->blocks[b], d->x1a.data() + o[0], d->x2a.data() + o[1], d->x3a.data() + o[2]);
+    if (rc) return cleanup(rc);
+  }
+  // halo transfer tables and reduction lists per group
+  std::vector<Ctrl*> all(nb);
+  for (int b = 0; b < nb; b++) all[b] = d->blocks[b]->ctrl;
+  for (int q = 0; q < ngroups; q++) {
+    mhdgb_domain::Group& G = d->g[q];
+    mhdgb_ensemble* e = d->groups[q];
+    if (cudaSetDevice(e->device) != cudaSuccess) return cleanup(MHDGB_ERR_CUDA);
+    std::vector<HaloXfer> xs;
+    std::vector<Ctrl*> own;
+    long long total = 0;
+    for (int b : gblocks[q]) {
+      mhdgb_solver* dst = d->blocks[b];
+      own.push_back(dst->ctrl);
+      const int c[3] = {b / (ntiles[1] * ntiles[2]), (b / ntiles[2]) % ntiles[1], b % ntiles[2]};
+      for (int f = 0; f < 6; f++) {
+        if (dst->cfg.bc[f] != MHDGB_BC_EXCHANGE) continue;
+        const int a = f >> 1, side = f & 1;
+        int cn[3] = {c[0], c[1], c[2]};
+        cn[a] = (c[a] + (side ? 1 : -1) + ntiles[a]) % ntiles[a];
+        mhdgb_solver* src = d->blocks[block_of(d, cn[0], cn[1], cn[2])];
+        HaloXfer t{};
+        const bool mixed = dst->kind == FUSED_MIXED;
+        for (int p = 0; p < 2; p++) {
+          t.src[p] = mixed ? (const void*)src->P32[p] : (const void*)src->P64[p];
+          t.dst[p] = mixed ? (void*)dst->P32[p] : (void*)dst->P64[p];
+        }
+        t.Ls = src->L;
+        t.Ld = dst->L;
+        t.bs = face_box(src->L, f ^ 1, false);  // the neighbour's layers next to its opposite face
+        t.bd = face_box(dst->L, f, true);
+        t.ctrl = dst->ctrl;
+        t.begin = total;
+        total += box_count(t.bd);
+        xs.push_back(t);
+      }
+    }
+    G.nxfer = (int)xs.size();
+    G.total = total;
+    G.nown = (int)own.size();
+    if ((!xs.empty() && cudaMalloc(&G.d_xfer, xs.size() * sizeof(HaloXfer)) != cudaSuccess) ||
+        cudaMalloc(&G.d_all, nb * sizeof(Ctrl*)) != cudaSuccess ||
+        cudaMalloc(&G.d_own, own.size() * sizeof(Ctrl*)) != cudaSuccess)
+      return cleanup(MHDGB_ERR_NOMEM);
+    if ((!xs.empty() && cudaMemcpy(G.d_xfer, xs.data(), xs.size() * sizeof(HaloXfer), cudaMemcpyHostToDevice) != cudaSuccess) ||
+        cudaMemcpy(G.d_all, all.data(), nb * sizeof(Ctrl*), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(G.d_own, own.data(), own.size() * sizeof(Ctrl*), cudaMemcpyHostToDevice) != cudaSuccess)
+      return cleanup(MHDGB_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&G.ev_step, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&G.ev_halo, cudaEventDisableTiming) != cudaSuccess)
+      return cleanup(MHDGB_ERR_CUDA);
+  }
+  *out = d;
+  return MHDGB_OK;
+}
+
+int mhdgb_domain_destroy(mhdgb_domain* d) {
+  if (!d) return MHDGB_OK;
+  for (size_t q = 0; q < d->groups.size(); q++) {
+    cudaSetDevice(d->group_dev[q]);
+    cudaStreamSynchronize(d->groups[q]->stream);
+  }
+  domain_destroy_graphs(d);
+  for (size_t q = 0; q < d->g.size(); q++) {
+    auto& G = d->g[q];
+    if (q < d->group_dev.size()) cudaSetDevice(d->group_dev[q]);
+    if (G.d_xfer) cudaFree(G.d_xfer);
+    if (G.d_all) cudaFree(G.d_all);
+    if (G.d_own) cudaFree(G.d_own);
+    if (G.ev_step) cudaEventDestroy(G.ev_step);
+    if (G.ev_halo) cudaEventDestroy(G.ev_halo);
+  }
+  for (auto* e : d->groups) mhdgb_ensemble_destroy(e);
+  delete d;
+  return MHDGB_OK;
+}
+
+const char* mhdgb_domain_last_error(const mhdgb_domain* d) { return d ? d->err.c_str() : "null domain"; }
+
+int mhdgb_domain_blocks(const mhdgb_domain* d) { return d ? (int)d->blocks.size() : 0; }
+
+int mhdgb_domain_block(mhdgb_domain* d, int b, mhdgb_solver** h, int offset[3], int extent[3]) {
+  if (!d || b < 0 || b >= (int)d->blocks.size()) return MHDGB_ERR_ARG;
+  if (h) *h = d->blocks[b];
+  for (int a = 0; a < 3; a++) {
+    if (offset) offset[a] = d->off[b][a];
+    if (extent) extent[a] = d->ext[b][a];
+  }
+  return MHDGB_OK;
+}
+
+// Whole-grid arrays: reference layout with the whole grid's extents (nx+5, ny+5, nz+5).
+int mhdgb_domain_upload_cons(mhdgb_domain* d, const double* U) {
+  if (!d || !U) return MHDGB_ERR_ARG;
+  const int IT = d->cfg.nx + 5, JT = d->cfg.ny + 5;
+  for (size_t b = 0; b < d->blocks.size(); b++) {
+    mhdgb_solver* h = d->blocks[b];
+    const auto& o = d->off[b];
+    const int it = h->L.itot, jt = h->L.jtot, kt = h->L.ktot;
+    std::vector<double> Ub((size_t)NCONS * it * jt * kt);
+    for (int k = 0; k < kt; k++)
+      for (int j = 0; j < jt; j++)
+        for (int m = 0; m < NCONS; m++)
+          std::memcpy(&Ub[(size_t)it * (m + (size_t)NCONS * (j + (size_t)jt * k))],
+                      &U[(size_t)o[0] + (size_t)IT * (m + (size_t)NCONS * ((j + o[1]) + (size_t)JT * (k + o[2])))],
+                      sizeof(double) * it);
+    int rc = mhdgb_upload_cons(h, Ub.data());
+    if (rc) return dfail(d, rc, "block " + std::to_string(b) + ": " + h->err);
+  }
+  d->prepared = false;
+  return MHDGB_OK;
+}
+
+// Interior cells of every block into the whole-grid array (its ghost cells are left as they are).
+int mhdgb_domain_download_cons(mhdgb_domain* d, double* U) {
+  if (!d || !U) return MHDGB_ERR_ARG;
+  const int IT = d->cfg.nx + 5, JT = d->cfg.ny + 5;
+  for (size_t b = 0; b < d->blocks.size(); b++) {
+    mhdgb_solver* h = d->blocks[b];
+    const auto& o = d->off[b];
+    const auto& x = d->ext[b];
+    const int it = h->L.itot, jt = h->L.jtot, kt = h->L.ktot;
+    std::vector<double> Ub((size_t)NCONS * it * jt * kt);
+    int rc = mhdgb_download_cons(h, Ub.data());
+    if (rc) return dfail(d, rc, "block " + std::to_string(b) + ": " + h->err);
+    for (int k = NGH; k < NGH + x[2]; k++)
+      for (int j = NGH; j < NGH + x[1]; j++)
+        for (int m = 0; m < NCONS; m++)
+          std::memcpy(&U[(size_t)(o[0] + NGH) + (size_t)IT * (m + (size_t)NCONS * ((j + o[1]) + (size_t)JT * (k + o[2])))],
+                      &Ub[(size_t)NGH + (size_t)it * (m + (size_t)NCONS * (j + (size_t)jt * k))], sizeof(double) * x[0]);
+  }
+  return MHDGB_OK;
+}
+
+int mhdgb_domain_init_kh(mhdgb_domain* d, unsigned long long seed, double vshear, double width, double bx,
+                         double amp, double sig, double noise) {
+  if (!d) return MHDGB_ERR_ARG;
+  const KhParams kp{seed, vshear, width, bx, amp, sig, noise};
+  for (size_t b = 0; b < d->blocks.size(); b++) {
+    const auto& o = d->off[b];
+    int rc = init_kh_block(d->blocks[b], d->cfg.nx, d->cfg.ny, o[0], o[1], o[2], kp);
+    if (rc) return dfail(d, rc, "block " + std::to_string(b) + ": " + d->blocks[b]->err);
+  }
+  d->prepared = false;
+  return MHDGB_OK;
+}
+
+int mhdgb_domain_prepare(mhdgb_domain* d) {
+  if (!d) return MHDGB_ERR_ARG;
+  return domain_prepare(d);
+}
+
+int mhdgb_domain_step(mhdgb_domain* d, int nsteps) {
+  if (!d || nsteps < 0) return MHDGB_ERR_ARG;
+  int rc;
+  // a block that lost its prepared state (new U, new physics) or whose kernel arguments changed
+  // since its group's launch table was built: prepare the whole domain again
+  bool stale = !d->prepared;
+  for (auto* h : d->blocks) stale = stale || !h->prepared;
+  for (auto* e : d->groups)
+    for (size_t i = 0; i < e->m.size(); i++)
+      stale = stale || i >= e->desc_seen.size() || e->desc_seen[i] != e->m[i]->desc_version;
+  if (stale && (rc = domain_prepare(d))) return rc;
+  const int G = 16;
+  if (d->groups.size() == 1 && nsteps >= G) {
+    mhdgb_ensemble* e = d->groups[0];
+    auto& Gr = d->g[0];
+    DCK(d, cudaSetDevice(e->device));
+    if (!Gr.gexec) {
+      cudaGraph_t graph = nullptr;
+      DCK(d, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+      rc = MHDGB_OK;
+      for (int s = 0; s < G && rc == MHDGB_OK; s++) rc = domain_step_once(d);
+      cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+      if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+      if (ce != cudaSuccess) return dfail(d, MHDGB_ERR_CUDA, "cudaStreamEndCapture");
+      ce = cudaGraphInstantiate(&Gr.gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) return dfail(d, MHDGB_ERR_CUDA, "cudaGraphInstantiate");
+    }
+    while (nsteps >= G) {
+      DCK(d, cudaGraphLaunch(Gr.gexec, e->stream));
+      nsteps -= G;
+    }
+  }
+  for (; nsteps > 0; nsteps--)
+    if ((rc = domain_step_once(d))) return rc;
+  for (auto* h : d->blocks) { h->p64_valid = false; h->p_user = false; }
+  return MHDGB_OK;
+}
+
+int mhdgb_domain_sync(mhdgb_domain* d, mhdgb_report* r) {
+  if (!d) return MHDGB_ERR_ARG;
+  int rc = domain_sync_streams(d);
+  if (rc) return rc;
+  int first = MHDGB_OK;
+  unsigned status = 0;
+  mhdgb_report r0{};
+  for (size_t b = 0; b < d->blocks.size(); b++) {
+    mhdgb_report rb{};
+    rc = mhdgb_sync(d->blocks[b], &rb);
+    status |= rb.status;
+    if (b == 0) r0 = rb;
+    if (rc && first == MHDGB_OK) first = dfail(d, rc, "block " + std::to_string(b) + ": " + d->blocks[b]->err);
+  }
+  r0.status = status;
+  if (r) *r = r0;
+  return first;
+}
+
+int mhdgb_domain_set_stop(mhdgb_domain* d, double tmax, long long max_steps) {
+  if (!d) return MHDGB_ERR_ARG;
+  for (size_t b = 0; b < d->blocks.size(); b++) {
+    int rc = mhdgb_set_stop(d->blocks[b], tmax, max_steps);
+    if (rc) return dfail(d, rc, d->blocks[b]->err);
+  }
+  return MHDGB_OK;
+}
+
+int mhdgb_domain_time_steps(mhdgb_domain* d, int nsteps, double* ms) {
+  if (!d || nsteps < 1 || !ms) return MHDGB_ERR_ARG;
+  int rc;
+  if (!d->prepared && (rc = domain_prepare(d))) return rc;
+  if (nsteps >= 16 && d->groups.size() == 1 && !d->g[0].gexec && (rc = mhdgb_domain_step(d, 16))) return rc;
+  if ((rc = domain_sync_streams(d))) return rc;
+  mhdgb_ensemble* e0 = d->groups[0];
+  DCK(d, cudaSetDevice(e0->device));
+  cudaEvent_t a, b;
+  DCK(d, cudaEventCreate(&a));
+  DCK(d, cudaEventCreate(&b));
+  DCK(d, cudaEventRecord(a, e0->stream));
+  // every group's stream starts after the first event, and the last event follows every group
+  for (size_t q = 1; q < d->groups.size(); q++) {
+    DCK(d, cudaSetDevice(d->groups[q]->device));
+    DCK(d, cudaStreamWaitEvent(d->groups[q]->stream, a, 0));
+  }
+  rc = mhdgb_domain_step(d, nsteps);
+  for (size_t q = 1; q < d->groups.size() && rc == MHDGB_OK; q++) {
+    DCK(d, cudaSetDevice(d->groups[q]->device));
+    DCK(d, cudaEventRecord(d->g[q].ev_step, d->groups[q]->stream));
+    DCK(d, cudaSetDevice(e0->device));
+    DCK(d, cudaStreamWaitEvent(e0->stream, d->g[q].ev_step, 0));
+  }
+  DCK(d, cudaSetDevice(e0->device));
+  DCK(d, cudaEventRecord(b, e0->stream));
+  DCK(d, cudaEventSynchronize(b));
+  float t = 0.0f;
+  DCK(d, cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = t;
+  return rc;
+}
+
+// KH diagnostic of the whole grid from the blocks' sums (each block's volume-weighted means,
+// recombined by volume).
+int mhdgb_domain_diag(mhdgb_domain* d, double out[3]) {
+  if (!d || !out) return MHDGB_ERR_ARG;
+  double v = 0.0, m = 0.0, a = 0.0;
+  for (size_t b = 0; b < d->blocks.size(); b++) {
+    double o[3];
+    int rc = mhdgb_diag(d->blocks[b], o);
+    if (rc) return dfail(d, rc, d->blocks[b]->err);
+    v += o[0];
+    m += o[1] * o[0];
+    a += o[2] * o[2] * o[0];
+  }
+  out[0] = v;
+  out[1] = m / v;
+  out[2] = std::sqrt(a / v);
   return MHDGB_OK;
 }
 

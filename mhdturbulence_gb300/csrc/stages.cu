@@ -236,24 +236,24 @@ __global__ void k_unpack(double* __restrict__ P, Layout L, PackBufs B, int bc_in
       // Br.Xs <- Bs.Xs (periodic) / Bs.Xe mirrored / Bs.Xe(0);  Br.Xe <- Bs.Xe / Bs.Xs mirrored / Bs.Xs(ngh-1)
       const double vin = bc_in == 3 ? B.xe[first] : fill_value(bc_in, B.xe, B.xs, t, mir, first, n, nve1);
       const double vout = bc_out == 3 ? B.xs[last] : fill_value(bc_out, B.xs, B.xe, t, mir, first, n, nve1);
-      P[L.at(NPRIM, n, k, j, i)] = vin;
-      P[L.at(NPRIM, n, k, j, ie + 1 + i)] = vout;
+      if (bc_in != BC_EXCHANGE) P[L.at(NPRIM, n, k, j, i)] = vin;
+      if (bc_out != BC_EXCHANGE) P[L.at(NPRIM, n, k, j, ie + 1 + i)] = vout;
     } else if (AX == 1) {
       mir = (((long long)n * kt + k) * NGH + (NGH - 1 - j)) * it + i;
       first = (((long long)n * kt + k) * NGH + 0) * it + i;
       last = (((long long)n * kt + k) * NGH + (NGH - 1)) * it + i;
       const double vin = bc_in == 3 ? B.ye[first] : fill_value(bc_in, B.ye, B.ys, t, mir, first, n, nve2);
       const double vout = bc_out == 3 ? B.ys[last] : fill_value(bc_out, B.ys, B.ye, t, mir, first, n, nve2);
-      P[L.at(NPRIM, n, k, j, i)] = vin;
-      P[L.at(NPRIM, n, k, je + 1 + j, i)] = vout;
+      if (bc_in != BC_EXCHANGE) P[L.at(NPRIM, n, k, j, i)] = vin;
+      if (bc_out != BC_EXCHANGE) P[L.at(NPRIM, n, k, je + 1 + j, i)] = vout;
     } else {
       mir = (((long long)n * NGH + (NGH - 1 - k)) * jt + j) * it + i;
       first = (((long long)n * NGH + 0) * jt + j) * it + i;
       last = (((long long)n * NGH + (NGH - 1)) * jt + j) * it + i;
       const double vin = bc_in == 3 ? B.ze[first] : fill_value(bc_in, B.ze, B.zs, t, mir, first, n, nve3);
       const double vout = bc_out == 3 ? B.zs[last] : fill_value(bc_out, B.zs, B.ze, t, mir, first, n, nve3);
-      P[L.at(NPRIM, n, k, j, i)] = vin;
-      P[L.at(NPRIM, n, ke + 1 + k, j, i)] = vout;
+      if (bc_in != BC_EXCHANGE) P[L.at(NPRIM, n, k, j, i)] = vin;
+      if (bc_out != BC_EXCHANGE) P[L.at(NPRIM, n, ke + 1 + k, j, i)] = vout;
     }
   }
 }

@@ -238,6 +238,14 @@ class Solver:
             raise MhdgbError(-1, f"variant_name: no variant {idx}")
         return name.decode()
 
+    def work_layout(self):
+        """(tiles in x, tiles in y, z chunk lengths) of the fused step's work queue."""
+        tx, ty, nc = C.c_int(), C.c_int(), C.c_int()
+        self._ck(self._L.mhdgb_work_layout(self._h, C.byref(tx), C.byref(ty), C.byref(nc), None), "work_layout")
+        ks = (C.c_int * (nc.value + 1))()
+        self._ck(self._L.mhdgb_work_layout(self._h, None, None, None, ks), "work_layout")
+        return tx.value, ty.value, [ks[i + 1] - ks[i] for i in range(nc.value)]
+
     def select_variant(self, idx):
         self._ck(self._L.mhdgb_select_variant(self._h, idx), "select_variant")
 
@@ -271,5 +279,32 @@ class Solver:
     def output(self, root, index, time, dt, ascii=False):
         self._ck(self._L.mhdgb_output(self._h, os.fsencode(root), index, time, dt, 1 if ascii else 0), "output")
 
+    # -- halo exchange of a block (faces shared with other blocks have the kind BC_EXCHANGE) --
+    def halo_bytes(self, face) -> int:
+        return int(self._L.mhdgb_halo_bytes(self._h, face))
+
+    def halo_pack(self, face, buf_ptr):
+        """Copy the 2 interior layers next to `face` into the device buffer at buf_ptr."""
+        self._ck(self._L.mhdgb_halo_pack(self._h, face, buf_ptr), f"halo_pack({face})")
+
+    def halo_unpack(self, face, buf_ptr):
+        """Copy the device buffer at buf_ptr into the 2 ghost layers beyond `face`."""
+        self._ck(self._L.mhdgb_halo_unpack(self._h, face, buf_ptr), f"halo_unpack({face})")
+
+    def get_reduction(self):
+        """(min cell CFL time, max signal speed) the next fused step will use (dt = cfl * the first)."""
+        a, b = C.c_double(), C.c_double()
+        self._ck(self._L.mhdgb_get_reduction(self._h, C.byref(a), C.byref(b)), "get_reduction")
+        return a.value, b.value
+
+    def set_reduction(self, dtmin, chmax):
+        self._ck(self._L.mhdgb_set_reduction(self._h, dtmin, chmax), "set_reduction")
+
     def init_kh(self, seed=1, vshear=0.5, width=0.05, bx=0.1, amp=1e-2, sig=0.2, noise=1e-4):
         self._ck(self._L.mhdgb_init_kh(self._h, seed, vshear, width, bx, amp, sig, noise), "init_kh")
+
+    def init_kh_block(self, whole, offset, seed=1, vshear=0.5, width=0.05, bx=0.1, amp=1e-2, sig=0.2, noise=1e-4):
+        """The KH state of this block of a whole grid (cell counts `whole`, first cell `offset`)."""
+        w, o = (C.c_int * 3)(*whole), (C.c_int * 3)(*offset)
+        self._ck(self._L.mhdgb_init_kh_block(self._h, w, o, seed, vshear, width, bx, amp, sig, noise),
+                 "init_kh_block")

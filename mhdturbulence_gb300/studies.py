@@ -3,6 +3,7 @@
     python -m mhdturbulence_gb300.studies turbulence [--n 256 --steps 200]
     python -m mhdturbulence_gb300.studies kh_growth  [--n 128 --tmax 6]
     python -m mhdturbulence_gb300.studies ensemble   [--members 64 --steps 20]
+    python -m mhdturbulence_gb300.studies low_beta   [--n 128 --steps 180]
     python -m mhdturbulence_gb300.studies all
 
 Each prints one JSON object per study.
@@ -160,6 +161,45 @@ def kh_growth(n=128, tmax=6.0, sample_every=200, low_beta_steps=None):
     return res
 
 
+def low_beta_sensitivity(n=128, steps=180, every=20, eps=1e-15, seed=11):
+    """How the low-beta KH variant (B_x = 1, p = 0.1) amplifies perturbations.  Four runs from the
+    same state: the separately rounded FP64 form (the reference's arithmetic), the FMA-contracted
+    FP64 form, the mixed form, and the separately rounded form started from the state with each
+    conserved value multiplied by (1 + eps * u), u uniform in [-1, 1] per cell (seeded).  Density L1
+    distances between pairs every `every` steps show whether the mixed form's distance from FP64 is
+    its own error or the scheme's amplification of any difference at the level of rounding."""
+    U0 = ic.prim_to_cons(ic.kh_prim(n, n, n, seed=1, bx=1.0, p=0.1), GAM)
+    rng = np.random.default_rng(seed)
+    Up = U0 * (1.0 + eps * rng.uniform(-1.0, 1.0, size=U0.shape))
+    runs = {"exact": ("fp64_exact", U0), "fma": ("fp64", U0), "mixed": ("mixed", U0), "perturbed": ("fp64_exact", Up)}
+    rho = {name: [] for name in runs}
+    marks = list(range(every, steps + 1, every))
+    for name, (prec, U) in runs.items():
+        with Solver(n, n, n, precision=prec) as s:
+            s.upload_cons(U)
+            done = 0
+            for m in marks:
+                s.step(m - done)
+                done = m
+                try:
+                    s.sync()
+                except MhdgbError:
+                    rho[name].append(None)
+                    break
+                rho[name].append(ic.interior(s.download_cons())[:, :, 0, :].copy())
+
+    def dist(a, b):
+        return [None if x is None or y is None else float(np.abs(x - y).sum() / np.abs(y).sum())
+                for x, y in zip(rho[a], rho[b])]
+    res = {"study": "low_beta_sensitivity", "n": n, "bx": 1.0, "p": 0.1, "steps": marks, "eps": eps,
+           "rho_l1_fma_vs_exact": dist("fma", "exact"), "rho_l1_mixed_vs_exact": dist("mixed", "exact"),
+           "rho_l1_mixed_vs_fma": dist("mixed", "fma"), "rho_l1_perturbed_vs_exact": dist("perturbed", "exact")}
+    pe = [v for v in res["rho_l1_perturbed_vs_exact"] if v]
+    if len(pe) >= 2:  # growth of the planted difference per step
+        res["perturbation_growth_per_step"] = float((pe[-1] / pe[0]) ** (1.0 / (marks[len(pe) - 1] - marks[0])))
+    return res
+
+
 def ensemble(members=64, steps=20, err_steps=50, big=512, seed=2026):
     specs = kh_ensemble_specs(members, seed=seed)
     res = {"study": "ensemble", "members": members, "cells": int(sum(s["nx"] * s["ny"] * s["nz"] for s in specs))}
@@ -195,7 +235,7 @@ def ensemble(members=64, steps=20, err_steps=50, big=512, seed=2026):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["turbulence", "kh_growth", "ensemble", "all"])
+    ap.add_argument("study", choices=["turbulence", "kh_growth", "ensemble", "low_beta", "all"])
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--tmax", type=float, default=6.0)
@@ -208,6 +248,8 @@ def main(argv=None):
             r = turbulence(n=a.n or 256, steps=a.steps or 200)
         elif st == "kh_growth":
             r = kh_growth(n=a.n or 128, tmax=a.tmax)
+        elif st == "low_beta":
+            r = low_beta_sensitivity(n=a.n or 128, steps=a.steps or 180)
         else:
             r = ensemble(members=a.members, steps=a.steps or 20, big=a.big)
         print(json.dumps(r), flush=True)

@@ -134,3 +134,24 @@ def test_new_grids_start_on_the_preferred_kernels():
             assert s.variant_name() == name, precision
         with Ensemble(kh_ensemble_specs(3, seed=5, sizes=(16, 24)), precision=precision) as ens:
             assert ens.variant_name == name, precision
+
+
+def test_work_queue_chunks_cover_the_grid():
+    """The z chunks of the work queue cover every plane once, shrink towards the end of the queue
+    where that balances the CTAs better, and do not change the results."""
+    for n, precision in ((150, "fp64"), (150, "mixed"), (256, "mixed"), (40, "fp64")):
+        with Solver(n, n, n, precision=precision) as s:
+            ntx, nty, chunks = s.work_layout()
+            assert sum(chunks) == n and min(chunks) >= 1 and len(chunks) <= 64, (n, precision, chunks)
+            assert ntx * 16 >= n and nty * 8 >= n
+    # same state with the grid's own chunking and with an ensemble's uniform 8-plane chunks
+    specs = [{"nx": 48, "ny": 40, "nz": 45, "mach": 0.4, "bx": 0.1, "seed": 1}]
+    with Ensemble(specs, precision="fp64") as ens, Solver(48, 40, 45, precision="fp64") as s:
+        ens.init_kh()
+        s.upload_cons(ens.members[0].download_cons())
+        assert s.work_layout()[2] != ens.members[0].work_layout()[2]
+        ens.step(9)
+        s.step(9)
+        ens.sync()
+        s.sync()
+        assert np.array_equal(ens.members[0].download_cons(), s.download_cons())
