@@ -280,6 +280,11 @@ int cuda_fail(mhdgb_solver* h, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
   } while (0)
 
+// cudaMemset and cudaMemcpy from pageable host memory run on the legacy default stream and may
+// still be in flight when they return; the handles' streams are non-blocking, so nothing orders
+// that work before theirs.  Every such call is followed by this wait.
+inline cudaError_t legacy_fence() { return cudaStreamSynchronize(cudaStreamLegacy); }
+
 template <class T>
 cudaError_t dalloc(mhdgb_solver* h, T** p, size_t n) {
   cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
@@ -287,6 +292,7 @@ cudaError_t dalloc(mhdgb_solver* h, T** p, size_t n) {
     h->bytes += n * sizeof(T);
     e = cudaMemset(*p, 0, n * sizeof(T));
   }
+  if (e == cudaSuccess) e = legacy_fence();
   return e;
 }
 
@@ -355,6 +361,7 @@ int upload_grid(mhdgb_solver* h) {
   CK(h, cudaMemcpy(h->dzsf, sz.data(), bf, cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->faces, h->x1a.data(), h->L.itot * sizeof(double), cudaMemcpyHostToDevice));
   CK(h, cudaMemcpy(h->faces + h->L.itot, h->x2a.data(), h->L.jtot * sizeof(double), cudaMemcpyHostToDevice));
+  CK(h, legacy_fence());
   return MHDGB_OK;
 }
 
@@ -1072,6 +1079,7 @@ int mhdgb_set_dt(mhdgb_solver* h, double dt) {
   int rc = set_device(h);
   if (rc) return rc;
   CK(h, cudaMemcpy(h->scal + 0, &dt, sizeof(double), cudaMemcpyHostToDevice));
+  CK(h, legacy_fence());
   return MHDGB_OK;
 }
 
@@ -1080,6 +1088,7 @@ int mhdgb_set_chg(mhdgb_solver* h, double chg) {
   int rc = set_device(h);
   if (rc) return rc;
   CK(h, cudaMemcpy(h->scal + 1, &chg, sizeof(double), cudaMemcpyHostToDevice));
+  CK(h, legacy_fence());
   return MHDGB_OK;
 }
 
@@ -1890,9 +1899,17 @@ int mhdgb_output_begin(mhdgb_solver* h, const char* root, int index, double time
   if (!h->have_state && !h->p_user) return fail(h, MHDGB_ERR_STATE, "no state uploaded");
   if ((rc = ensure_snapshot_bufs(h))) return rc;
   // A primitive array the caller uploaded is written as it is (the reference writes its P, which
-  // for the initial state is GenerateProblem's); otherwise the primitives are recovered from U in
-  // stream order, after every step already enqueued.
-  const double* P = h->p_user ? h->P64[cur_index(h)] : nullptr;
+  // for the initial state is GenerateProblem's), and so is the FP64 fused step's own recovery once
+  // the handle steps fused (the P that mhdgb_download_prim returns; the parity of the current
+  // buffer is known after the steps already enqueued have run); otherwise the primitives are
+  // recovered from U in stream order, after every step already enqueued.
+  const double* P = nullptr;
+  if (h->p_user) {
+    P = h->P64[cur_index(h)];
+  } else if (h->prepared && h->kind != FUSED_MIXED) {
+    if ((rc = settle(h))) return rc;
+    P = h->P64[cur_index(h)];
+  }
   CK(h, launch_snapshot(h->U, P, h->L, h->cfg.gam, h->d_snap, h->stream));
   CK(h, cudaEventRecord(h->ev_packed, h->stream));
   CK(h, cudaStreamWaitEvent(h->copy_stream, h->ev_packed, 0));
@@ -2503,7 +2520,8 @@ int mhdgb_domain_create(const mhdgb_config* cfg, const int ntiles[3], int ngroup
       return cleanup(MHDGB_ERR_NOMEM);
     if ((!xs.empty() && cudaMemcpy(G.d_xfer, xs.data(), xs.size() * sizeof(HaloXfer), cudaMemcpyHostToDevice) != cudaSuccess) ||
         cudaMemcpy(G.d_all, all.data(), nb * sizeof(Ctrl*), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(G.d_own, own.data(), own.size() * sizeof(Ctrl*), cudaMemcpyHostToDevice) != cudaSuccess)
+        cudaMemcpy(G.d_own, own.data(), own.size() * sizeof(Ctrl*), cudaMemcpyHostToDevice) != cudaSuccess ||
+        legacy_fence() != cudaSuccess)
       return cleanup(MHDGB_ERR_CUDA);
     if (cudaEventCreateWithFlags(&G.ev_step, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&G.ev_halo, cudaEventDisableTiming) != cudaSuccess)

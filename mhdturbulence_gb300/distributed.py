@@ -13,6 +13,7 @@ A rank's block is any object with the block interface (GpuBlock here: a Solver o
     prepare()        recover P from U, fill the ghosts of non-exchanged faces, reduce dt / c_h locally
     step()           one step with the pending (global) dt / c_h, ending as prepare() does
     pack(face)       the 2 interior layers next to `face` (a tensor on the transport's device)
+    recv_buffer(face)  (optional) an empty tensor that unpack(face, .) takes without a copy
     unpack(face, t)  into the 2 ghost layers beyond `face`
     get_reduction() / set_reduction(dtmin, chmax)   the pending reduction (dt = cfl * dtmin)
     sync()           a Report (step, time, dt, c_h, status)
@@ -97,6 +98,9 @@ class GpuBlock:
         self.solver.halo_pack(face, t.data_ptr())
         return t
 
+    def recv_buffer(self, face):
+        return self._buffer(face)
+
     def unpack(self, face, t):
         import torch
         if self.transport == "cuda":
@@ -142,7 +146,9 @@ class DistributedGrid:
         import torch
         dist = self.dist
         sends = {f: self.block.pack(f) for f, _ in self.links}
-        recvs = {f: torch.empty_like(sends[f]) for f, _ in self.links}
+        # page-locked for a host transport (empty_like of a page-locked tensor is pageable)
+        alloc = getattr(self.block, "recv_buffer", None)
+        recvs = {f: alloc(f) if alloc else torch.empty_like(sends[f]) for f, _ in self.links}
         ops = [dist.P2POp(dist.isend, sends[f], peer, self.group, tag=f) for f, peer in self.links]
         ops += [dist.P2POp(dist.irecv, recvs[f], peer, self.group, tag=f ^ 1)
                 for f, peer in sorted(self.links, key=lambda fp: fp[0] ^ 1)]
