@@ -25,12 +25,14 @@ struct FusedSmemFS {
   static constexpr int NFX = NCONS * TY * (TX + 1);  // x faces i in [0, TX]
   static constexpr int NFY = NCONS * (TY + 1) * TX;  // y faces j in [0, TY]
   static constexpr int NFZ = NCONS * TY * TX;        // z faces k+1/2
-  static constexpr int NF = NFX + NFY + NFZ;         // one face buffer
+  static constexpr int NXY = NFX + NFY;              // one buffer of x and y faces
   static constexpr size_t a16(size_t x) { return (x + 15) / 16 * 16; }
   static constexpr size_t ring_off = 0;
   static constexpr size_t f_off = ((size_t)NBUF * PLANE * sizeof(R) + 127) / 128 * 128;
-  static constexpr size_t low_off = f_off + a16(2 * (size_t)NF * sizeof(R));  // faces kb-1/2 of a chunk
-  static constexpr size_t red_off = low_off + a16(NFZ * sizeof(R));
+  // z faces in three buffers by plane: the cells of plane k read faces k-1/2 and k+1/2 while the
+  // faces k+3/2 of the next plane are formed
+  static constexpr size_t z_off = f_off + a16(2 * (size_t)NXY * sizeof(R));
+  static constexpr size_t red_off = z_off + a16(3 * (size_t)NFZ * sizeof(R));
   static constexpr size_t bar_off = red_off + 64 * sizeof(double);
   static constexpr size_t misc_off = bar_off + NBUF * sizeof(uint64_t);  // item, abort, 2 face counters
   static constexpr size_t used = misc_off + 16;
@@ -54,7 +56,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations
   R* ring = reinterpret_cast<R*>(smem + S::ring_off);
   R* fbuf = reinterpret_cast<R*>(smem + S::f_off);
-  R* low = reinterpret_cast<R*>(smem + S::low_off);
+  R* zbuf = reinterpret_cast<R*>(smem + S::z_off);
   double* red = reinterpret_cast<double*>(smem + S::red_off);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::bar_off);
   int& s_item = *reinterpret_cast<int*>(smem + S::misc_off);
@@ -71,9 +73,16 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
   }
   __syncthreads();
 
-  unsigned fills[NBUF];  // loads issued per slot (identical in every thread)
-#pragma unroll
-  for (int s = 0; s < NBUF; s++) fills[s] = 0;
+  // Loads issued per slot, as bit masks (identical in every thread; registers, where an array
+  // indexed by the run-time slot would live in local memory): bit s of odd = slot s has had an odd
+  // number of loads, bit s of used = slot s has had one at all.  The wait for the latest load of
+  // slot s is on mbarrier phase parity (count - 1) & 1 = 1 - odd bit.
+  unsigned odd = 0, used = 0;
+  auto fill = [&](int s) {
+    odd ^= 1u << s;
+    used |= 1u << s;
+  };
+  auto parity = [&](int s) { return ((odd >> s) & 1u) ^ 1u; };
   const int oi = tid % TX, oj = tid / TX;  // owner column of this thread (if oj < TY)
 
   for (;;) {
@@ -120,17 +129,16 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
     };
     auto wait_plane = [&](int p) {
       const int s = slot_of(p);
-      if (!mbar_wait(&bars[s], (fills[s] - 1) & 1, &ctrl->status)) s_abort = 1;
+      if (!mbar_wait(&bars[s], parity(s), &ctrl->status)) s_abort = 1;
     };
     auto PV0 = [&](const R* pl, int i, int j) -> const R& { return pl[((j + 2) * NPRIM) * PX + (i + 2)]; };
-    auto FXS = [&](int b, int m, int i, int j) -> R& { return fbuf[b * S::NF + (m * TY + j) * (TX + 1) + i]; };
+    auto FXS = [&](int b, int m, int i, int j) -> R& { return fbuf[b * S::NXY + (m * TY + j) * (TX + 1) + i]; };
     auto FYS = [&](int b, int m, int i, int j) -> R& {
-      return fbuf[b * S::NF + S::NFX + (m * (TY + 1) + j) * TX + i];
+      return fbuf[b * S::NXY + S::NFX + (m * (TY + 1) + j) * TX + i];
     };
-    auto FZS = [&](int b, int m, int i, int j) -> R& {
-      return fbuf[b * S::NF + S::NFX + S::NFY + (m * TY + j) * TX + i];
-    };
-    auto LOW = [&](int m, int i, int j) -> R& { return low[(m * TY + j) * TX + i]; };
+    // z face p+1/2 (p = kb-1 .. ke-1) lives in z buffer (p - kb + 1) % 3
+    auto zslot = [&](int p) { return (p - kb + 1) % 3; };
+    auto FZS = [&](int z, int m, int i, int j) -> R& { return zbuf[z * S::NFZ + (m * TY + j) * TX + i]; };
 
     // prologue: planes kb-2 .. kb+3 (those up to ke+1; ke >= kb+1, so kb+2 always exists)
     if (tid == 0) {
@@ -139,12 +147,11 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
       fence_proxy_async();
       for (int p = kb - 2; p <= kb + 3 && p <= ke + 1; p++) issue(p);
     }
-    for (int p = kb - 2; p <= kb + 3 && p <= ke + 1; p++) fills[slot_of(p)]++;
+    for (int p = kb - 2; p <= kb + 3 && p <= ke + 1; p++) fill(slot_of(p));
     for (int p = kb - 2; p <= kb + 2; p++) wait_plane(p);
     __syncthreads();
     if (s_abort) break;
 
-    R fz_lo[NCONS];  // flux through face k-1/2 of the owner's column
     const int nxf = cy * (cx + 1), nyf = (cy + 1) * cx, nzf = cy * cx;
     const FastDiv dv0(cx), dv1(cx + 1);
 
@@ -156,7 +163,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
       }
       if (k > kb) wait_plane(k + 2);
       const int fb = k & 1;
-      // ---- faces of plane k (on the first plane also the faces kb-1/2, into LOW) ----
+      // ---- faces of plane k (on the first plane also the faces kb-1/2) ----
       // One unpadded list over x, y and z faces, each read in its rotated frame (see k_fused_step).
       // Warp items come from counter fb; thread 0 clears the other one, which plane k-1 used and
       // plane k+1 will use, and the barrier below publishes it.
@@ -202,7 +209,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
             c1 = &PV0(plane(kl), i, j);
             c2 = &PV0(plane(kl + 1), i, j);
             c3 = &PV0(plane(kl + 2), i, j);
-            fo = lower ? &LOW(0, i, j) : &FZS(fb, 0, i, j);
+            fo = &FZS(zslot(kl), 0, i, j);
             fstr = TY * TX;
           }
           const int u1 = unrot_comp(1, rot), u2 = unrot_comp(2, rot);
@@ -240,21 +247,18 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
           fence_proxy_async();
           issue(kb + 4);
         }
-        fills[slot_of(kb + 4)]++;
+        fill(slot_of(kb + 4));
       }
       if (k + 5 <= ke + 1) {  // plane k-1's slot
         if (tid == 0) {
           fence_proxy_async();
           issue(k + 5);
         }
-        fills[slot_of(k + 5)]++;
+        fill(slot_of(k + 5));
       }
       // ---- cells of plane k: update, recovery, ghost images, candidates (as k_fused_step) ----
       if (own) {
-        if (k == kb) {
-#pragma unroll
-          for (int m = 0; m < NCONS; m++) fz_lo[m] = LOW(m, oi, oj);
-        }
+        const int zl = zslot(k - 1), zh = zslot(k);
         DivAcc<R> acc;
         const R xi = inv_of<R>(a, 0, ii + NGH);
         const R yi = inv_of<R>(a, 1, (a.quirk ? ii : jj) + NGH);
@@ -263,9 +267,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
         for (int m = 0; m < NCONS; m++) {
           acc.first(m, FXS(fb, m, oi + 1, oj) - FXS(fb, m, oi, oj), xi);
           acc.add(m, FYS(fb, m, oi, oj + 1) - FYS(fb, m, oi, oj), yi);
-          const R fzh = FZS(fb, m, oi, oj);
-          acc.add(m, fzh - fz_lo[m], zi);
-          fz_lo[m] = fzh;
+          acc.add(m, FZS(zh, m, oi, oj) - FZS(zl, m, oi, oj), zi);
         }
         const size_t cu = L.at(NCONS, 0, k + NGH, jj + NGH, ii + NGH);
         double u[NCONS];
@@ -293,7 +295,7 @@ k_fused_step_fs(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ 
   if (s_abort) {
     // drain: wait (bounded) for any load still in flight before leaving
     for (int s = 0; s < NBUF; s++)
-      if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &desc[0].a.ctrl->status);
+      if ((used >> s) & 1u) mbar_wait(&bars[s], parity(s), &desc[0].a.ctrl->status);
   }
   if (tid == 0) fused_finish_cta(desc, lc, ninst);
 }

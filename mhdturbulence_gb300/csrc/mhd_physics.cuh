@@ -264,9 +264,10 @@ template <> struct Dir<3> {
 
 // Dir<0>: the face's primitives arrive rotated already (normal, first and second tangential
 // components in the slots of x, y, z, as Dir<1> reads them), for the fused step's direction-generic
-// face list.  rot = 0, 1, 2 for x, y, z faces; the one place it enters the arithmetic is the sums
-// over the three components, which keep the unrotated x, y, z order (sum_sq3), so a Dir<0> flux is
-// bit for bit the Dir<1/2/3> flux of the same face.
+// face list.  rot = 0, 1, 2 for x, y, z faces; the one place it enters the FP64 arithmetic is the
+// sums over the three components, which keep the unrotated x, y, z order (sum_sq3), so an FP64
+// Dir<0> flux is bit for bit the Dir<1/2/3> flux of the same face.  The FP32 solver sums in the
+// rotated order (no selects; every FP32 kernel uses the same order, so they agree bit for bit).
 template <> struct Dir<0> : Dir<1> {};
 
 // Unrotated component (0, 1, 2 = x, y, z) held in rotated slot 0, 1, 2 of a face with rotation rot.
@@ -275,7 +276,7 @@ __device__ __forceinline__ int unrot_comp(int slot, int rot) { return slot + rot
 // P[b]^2 + P[b+1]^2 + P[b+2]^2 over unrotated components x, y, z in that order.
 template <int DIR, class R>
 __device__ __forceinline__ R sum_sq3(const R (&P)[NPRIM], int b, int rot) {
-  if constexpr (DIR != 0) {
+  if constexpr (DIR != 0 || std::is_same<R, float>::value) {
     return P[b] * P[b] + P[b + 1] * P[b + 1] + P[b + 2] * P[b + 2];
   } else {
     const R r0 = P[b], r1 = P[b + 1], r2 = P[b + 2];
@@ -361,16 +362,12 @@ struct PairHi {
 
 // prim2cons_state of a face's two states at once (FP32, rotated frame as Dir<0>): P[n] holds the
 // left and right primitive, C[q] receives the two state vectors, with packed FP32 instructions (two
-// lanes per instruction) and a fixed order of operations; the sums over the components keep the
-// unrotated x, y, z order as sum_sq3 does.
-__device__ __forceinline__ void prim2cons_state_pair(const float2 (&P)[NPRIM], float2 (&C)[NVEC], int rot) {
+// lanes per instruction) and a fixed order of operations; the sums over the components are in the
+// rotated order, as sum_sq3 forms them in FP32.
+__device__ __forceinline__ void prim2cons_state_pair(const float2 (&P)[NPRIM], float2 (&C)[NVEC], int) {
   const float2 half = make_float2(0.5f, 0.5f);
-  auto sq3 = [&](int b) {  // P[b]^2 + P[b+1]^2 + P[b+2]^2 in the unrotated order
-    const float2 r0 = P[b], r1 = P[b + 1], r2 = P[b + 2];
-    const float2 x = rot == 0 ? r0 : (rot == 1 ? r2 : r1);
-    const float2 y = rot == 0 ? r1 : (rot == 1 ? r0 : r2);
-    const float2 z = rot == 0 ? r2 : (rot == 1 ? r1 : r0);
-    return __ffma2_rn(z, z, __ffma2_rn(y, y, __fmul2_rn(x, x)));
+  auto sq3 = [&](int b) {  // P[b]^2 + P[b+1]^2 + P[b+2]^2
+    return __ffma2_rn(P[b + 2], P[b + 2], __ffma2_rn(P[b + 1], P[b + 1], __fmul2_rn(P[b], P[b])));
   };
   const float2 rho = P[nden];
   const float2 rinv = make_float2(rcp_approx_f32(rho.x), rcp_approx_f32(rho.y));
