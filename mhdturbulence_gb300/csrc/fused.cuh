@@ -344,9 +344,16 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
   }
   __syncthreads();
 
-  unsigned fills[NBUF];  // loads issued per slot (identical in every thread)
-#pragma unroll
-  for (int s = 0; s < NBUF; s++) fills[s] = 0;
+  // Loads issued per slot, as bit masks (identical in every thread; registers, where an array
+  // indexed by the run-time slot would live in local memory): bit s of odd = slot s has had an odd
+  // number of loads, bit s of used = slot s has had one at all.  The wait for the latest load of
+  // slot s is on mbarrier phase parity (count - 1) & 1 = 1 - odd bit.
+  unsigned odd = 0, used = 0;
+  auto fill = [&](int s) {
+    odd ^= 1u << s;
+    used |= 1u << s;
+  };
+  auto parity = [&](int s) { return ((odd >> s) & 1u) ^ 1u; };
   const int oi = tid % TX, oj = tid / TX;  // owner column of this thread (if oj < TY)
 
   for (;;) {
@@ -393,7 +400,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     };
     auto wait_plane = [&](int p) {
       const int s = slot_of(p);
-      if (!mbar_wait(&bars[s], (fills[s] - 1) & 1, &ctrl->status)) s_abort = 1;
+      if (!mbar_wait(&bars[s], parity(s), &ctrl->status)) s_abort = 1;
     };
     auto PV = [&](const R* pl, int n, int i, int j) -> R { return pl[((j + 2) * NPRIM + n) * PX + (i + 2)]; };
     auto PV0 = [&](const R* pl, int i, int j) -> const R& { return pl[((j + 2) * NPRIM) * PX + (i + 2)]; };
@@ -410,7 +417,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       for (int p = kb - 2; p < kb + 2; p++) issue(p);
     }
 #pragma unroll
-    for (int s = 0; s < NBUF; s++) fills[s]++;
+    for (int s = 0; s < NBUF; s++) fill(s);
     for (int p = kb - 2; p < kb + 2; p++) wait_plane(p);
     __syncthreads();
     if (s_abort) break;
@@ -434,7 +441,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       fence_proxy_async();
       if (kb + 2 <= ke + 1) issue(kb + 2);
     }
-    if (kb + 2 <= ke + 1) fills[slot_of(kb + 2)]++;
+    if (kb + 2 <= ke + 1) fill(slot_of(kb + 2));
 
     // work-list sizes (the slope sub-lists padded to whole warps) and the divisors of their decode
     const FastDiv dv0(cx), dv1(cx + 1), dv2(cx + 2);
@@ -576,14 +583,14 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
           fence_proxy_async();
           issue(kb + 3);
         }
-        fills[slot_of(kb + 3)]++;
+        fill(slot_of(kb + 3));
       }
       if (k + 4 <= ke + 1) {  // plane k's slot
         if (tid == 0) {
           fence_proxy_async();
           issue(k + 4);
         }
-        fills[slot_of(k + 4)]++;
+        fill(slot_of(k + 4));
       }
       // ---- phase C: cell update, recovery, ghost images, candidates ----
       if (own) {
@@ -635,7 +642,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
   if (s_abort) {
     // drain: wait (bounded) for any load still in flight before leaving
     for (int s = 0; s < NBUF; s++)
-      if (fills[s]) mbar_wait(&bars[s], (fills[s] - 1) & 1, &desc[0].a.ctrl->status);
+      if ((used >> s) & 1u) mbar_wait(&bars[s], parity(s), &desc[0].a.ctrl->status);
   }
   if (tid == 0) fused_finish_cta(desc, lc, ninst);
 }

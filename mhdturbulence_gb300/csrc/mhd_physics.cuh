@@ -461,10 +461,12 @@ __device__ __forceinline__ void hlld(const R (&leftst)[NVEC], const R (&rigtst)[
   const R bxsq = bxs * bxs;
   // Degenerate star states (rho (S - v)(S - S_M) = B_x^2, e.g. field-aligned flow with c_f = v_A):
   // the reference switches to v* = v, B* = B below |T| < 1e-30, which FP64 rounding noise (~1e-16)
-  // never reaches.  In FP32 both T and the numerators it divides are rounding noise (~1e-7) there,
-  // so the FP32 solver treats |T| < 3e-4 p_T* (about the square root of FP32's epsilon, relative
-  // to the star total pressure) as degenerate; faces with B_n ~ 0 have T ~ rho c_f^2, far above.
-  const R deg = std::is_same<R, float>::value ? smax(eps, R(3e-4) * fabs(ptst)) : eps;
+  // never reaches.  In FP32, T and the numerators it divides are rounding noise (~1e-7 of p_T*)
+  // near degeneracy, so the FP32 solver treats |T| < 1e-6 p_T* (about eight FP32 ulps of the star
+  // total pressure) as degenerate.  Above that the FP32 star state still follows FP64's: on the
+  // low-beta KH layer (B_x = 1, p = 0.1) thresholds from 3e-7 to 3e-6 give the same state, while
+  // 1e-5 and above switch faces the FP64 solver resolves, and its absolute 1e-30 fails in FP32.
+  const R deg = std::is_same<R, float>::value ? smax(eps, R(1e-6) * fabs(ptst)) : eps;
   R temp_fst = rosdl * sdml - bxsq;
   R sign1 = copysign(R(1), fabs(temp_fst) - deg);
   R maxs1 = smax(R(0), sign1);
@@ -611,7 +613,7 @@ __device__ __forceinline__ void hlld_branch(const CL& leftst, const CR& rigtst, 
   R rost = ro, vxst = vx, vyst = vy, vzst = vz, byst = by, bzst = bz;
   const R temp_fst = rosd * sdm - bxsq;
   // FP32: the degenerate-state guard relative to the star total pressure (see hlld())
-  const R deg = std::is_same<R, float>::value ? imax(eps, R(3e-4) * fabs(ptst)) : eps;
+  const R deg = std::is_same<R, float>::value ? imax(eps, R(1e-6) * fabs(ptst)) : eps;
   const bool nondeg = !abs_less(temp_fst, deg);
   R isdm = R(0);
   if (nondeg) {
