@@ -69,6 +69,14 @@ __device__ __forceinline__ float rcp_approx_f32(float x) {
   return r;
 }
 
+// Separately rounded multiply, add and subtract (never contracted into an FMA).
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+
 // Narrowing and widening for FP32 seeds only.  The callers have checked that the argument is a
 // finite normal number well inside the float range, and a seed needs no rounding (the Newton steps
 // that follow remove its error), so the narrowing truncates the mantissa (error < 2^-23) and the
@@ -591,7 +599,12 @@ __device__ __forceinline__ void hlld_branch(const CL& leftst, const CR& rigtst, 
   const R rosdl = rol * sdl;
   const R rosdr = ror * sdr;
   const R tden = fdiv(R(1), rosdr - rosdl);
-  const R sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * tden;
+  // The contact speed decides the upwind side, and the reference's fluxes differ on the two sides of
+  // S_M = 0 when B_n != 0 (e.g. the energy flux at a reflecting wall, whose two states are mirror
+  // images).  There the reference's separately rounded products cancel to exactly +0 and it takes
+  // the left side; an FMA-contracted numerator would leave the rounding error of one product, of
+  // either sign.  So the numerator is formed from separately rounded products, as the reference does.
+  const R sm = rn_mul(rn_add(rn_add(rn_sub(rn_mul(rosdr, vxr), rn_mul(rosdl, vxl)), -ptr), ptl), tden);
   const R ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * tden;
   const R bxs = R(0.5) * (leftst[mubu] + rigtst[mubu]);
   const R bxsq = bxs * bxs;
@@ -764,7 +777,8 @@ __device__ __forceinline__ void hllc(const R (&leftst)[NVEC], const R (&rigtst)[
   const R sdl = sl - vxl, sdr = sr - vxr;
   const R rosdl = rol * sdl, rosdr = ror * sdr;
   const R temp = fdiv(R(1), rosdr - rosdl);
-  const R sm = (rosdr * vxr - rosdl * vxl - ptr + ptl) * temp;
+  // separately rounded, so mirror-image states give exactly +0 as in the reference (see hlld_branch)
+  const R sm = rn_mul(rn_add(rn_add(rn_sub(rn_mul(rosdr, vxr), rn_mul(rosdl, vxl)), -ptr), ptl), temp);
   const R sdml = sl - sm, isdml = fdiv(R(1), sdml);
   const R sdmr = sr - sm, isdmr = fdiv(R(1), sdmr);
   const R ptst = (rosdr * ptl - rosdl * ptr + rosdl * rosdr * (vxr - vxl)) * temp;
