@@ -21,9 +21,10 @@ arithmetic restated in C, OpenMP) on this host's cores.
 
 --impl reference times the reference's CPU path on the host cores: the reference sources cannot
 be built on this machine (they need Kokkos and MPI, and the reference tree is absent here), so the
-oracle port stands in for it, with all host threads.  On the same cores the port runs 1.34x as fast
-as the reference's own stages built against a Kokkos/MPI shim (oracle/cpu_baseline_fidelity.py),
-so the ratio against this arm understates the speed-up over the reference itself.
+oracle port stands in for it, with all host threads.  On the same cores (KH 150^3, 8 threads, best of
+3 runs of 6 steps) the port runs 1.08x as fast as the reference's own stages built against a
+Kokkos/MPI shim, with equal final states (oracle/cpu_baseline_fidelity.py), so the ratio against this
+arm understates the speed-up over the reference itself by about that factor.
 
 Multi-GPU (torchrun): the ranks hold the 150^3 blocks of one 150 x 150 x (150 N) KH grid split
 along z and swap the halos of their shared faces over NCCL after every step, with dt and c_h
