@@ -133,6 +133,18 @@ __device__ __forceinline__ void block_reduce_to_slot(double mn, double mx, doubl
   __syncthreads();
 }
 
+// Named CTA barrier `id` (1..15) of `nthreads` threads (whole warps): warps that only signal
+// arrive without waiting, warps that need the others' shared-memory writes wait (bar.sync) until
+// every participant has arrived; writes made before an arrive are visible after the wait.  Each
+// participating warp must reach its arrive or its wait exactly once per use, in uniform control
+// flow, and a use must complete before the next one begins.
+__device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // ---------------------------------------------------------------------------------------------
 // mbarrier + TMA (cp.async.bulk.tensor) helpers.  Waits are bounded: on timeout the waiter sets
 // ST_TIMEOUT in the status word and gives up instead of spinning forever.

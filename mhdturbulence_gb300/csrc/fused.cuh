@@ -18,7 +18,10 @@
 // The slope list is padded per direction to whole warps (no warp mixes two code paths) and handed
 // out per warp from a shared counter; the face list is one unpadded list over all directions,
 // each face read in its rotated frame by direction-generic code.  Masked-off lanes cost the FP64
-// pipe as much as active ones, so padding is paid for in full.
+// pipe as much as active ones, so padding is paid for in full.  In the FP64 form the warps that
+// own no cell start the next plane's phase A as soon as their own faces are formed (a named
+// barrier that only the owner warps wait at), into a second x/y slope buffer and a third z-slope
+// buffer, so their FP64 pipe does not idle while the last faces are formed.
 // Step n reads dt and c_h from ctrl->slot[n%3] (made by step n-1 or by the initial reduction),
 // reduces into slot[(n+1)%3] and resets slot[(n+2)%3]; the last CTA to finish advances the step
 // counter and the simulated time.  All launches of a run are identical and can be captured once in
@@ -40,7 +43,18 @@
 
 namespace mhdgb {
 
-template <class R, int TX, int TY, int NT>
+// Bytes of the fused kernel's shared memory for nslb x/y slope buffers (see FusedSmem).
+constexpr size_t fused_smem_bytes(int TX, int TY, size_t rsz, int nslb) {
+  const size_t PLANE = (size_t)(TX + 4) * NPRIM * (TY + 4);
+  const size_t NSLX = (size_t)NPRIM * TY * (TX + 2), NSLY = (size_t)NPRIM * (TY + 2) * TX,
+               NSLZ = (size_t)NPRIM * TY * TX;
+  const size_t NFX = (size_t)NCONS * TY * (TX + 1), NFY = (size_t)NCONS * (TY + 1) * TX, NFZ = (size_t)NCONS * TY * TX;
+  auto a16 = [](size_t x) { return (x + 15) / 16 * 16; };
+  return (4 * PLANE * rsz + 127) / 128 * 128 + nslb * (a16(NSLX * rsz) + a16(NSLY * rsz)) + a16(3 * NSLZ * rsz) +
+         a16(NFX * rsz) + a16(NFY * rsz) + a16(NFZ * rsz) + 64 * sizeof(double) + 4 * sizeof(uint64_t) + 16 + 128;
+}
+
+template <class R, int TX, int TY, int NT, int MINB = 1>
 struct FusedSmem {
   static constexpr int NBUF = 4;
   static constexpr int PX = TX + 4, PY = TY + 4;
@@ -51,22 +65,34 @@ struct FusedSmem {
   static constexpr int NFX = NCONS * TY * (TX + 1);         // x faces i in [0, TX]
   static constexpr int NFY = NCONS * (TY + 1) * TX;         // y faces j in [0, TY]
   static constexpr int NFZ = NCONS * TY * TX;               // z faces k+1/2
+  // Owner threads: the whole warps that hold the tile's cell columns.  OV: the warps without a
+  // column start the next plane's slopes as soon as their own faces are formed, while the others
+  // still form faces, so the x and y slopes get one buffer per plane parity.  Only in the FP64 form
+  // (where the faces' FP64-pipe time is uneven over the SM sub-partitions: 2 % faster at 150^3;
+  // the FP32 variants ran 3 % slower), where there are such warps, and where the second buffer
+  // keeps MINB CTAs per SM.
+  static constexpr int NOWN = (TX * TY + 31) / 32 * 32;
+  static constexpr bool OV = sizeof(R) == sizeof(double) && NT > NOWN &&
+                             MINB * (fused_smem_bytes(TX, TY, sizeof(R), 2) + 1024) <= 228 * 1024;
+  static constexpr int NSLB = OV ? 2 : 1;
   static constexpr size_t a16(size_t x) { return (x + 15) / 16 * 16; }
   static constexpr size_t ring_off = 0;
   static constexpr size_t slx_off = ((size_t)NBUF * PLANE * sizeof(R) + 127) / 128 * 128;
-  static constexpr size_t sly_off = slx_off + a16(NSLX * sizeof(R));
-  static constexpr size_t slz_off = sly_off + a16(NSLY * sizeof(R));
-  // three z-slope planes: the current and next plane's, and plane kb-1's at the start of a chunk
+  static constexpr size_t sly_off = slx_off + NSLB * a16(NSLX * sizeof(R));
+  static constexpr size_t slz_off = sly_off + NSLB * a16(NSLY * sizeof(R));
+  // three z-slope planes, rotating: while the faces of plane k read the z slopes of planes k and
+  // k+1, those of plane k+2 are formed; at the start of a chunk the third buffer holds plane kb-1's
   // (whose column-owned entries then hold the flux through face kb-1/2)
   static constexpr size_t fx_off = slz_off + a16(3 * NSLZ * sizeof(R));
   static constexpr size_t fy_off = fx_off + a16(NFX * sizeof(R));
   static constexpr size_t fz_off = fy_off + a16(NFY * sizeof(R));
   static constexpr size_t red_off = fz_off + a16(NFZ * sizeof(R));
   static constexpr size_t bar_off = red_off + 64 * sizeof(double);
-  static constexpr size_t misc_off = bar_off + NBUF * sizeof(uint64_t);  // work item, abort flag
+  static constexpr size_t misc_off = bar_off + NBUF * sizeof(uint64_t);  // work item, abort flag, 2 slope counters
   static constexpr size_t used = misc_off + 16;
   static constexpr size_t total = used + 128;  // room to align the base to 128 bytes
   static constexpr unsigned plane_tx_bytes = (unsigned)(PLANE * sizeof(R));
+  static_assert(total == fused_smem_bytes(TX, TY, sizeof(R), NSLB), "layout and size formula agree");
   static_assert(NT % 32 == 0 && NT >= TX * TY, "one owner thread per column, whole warps");
   static_assert((TX * sizeof(R)) % 16 == 0, "TMA x offsets must be 16-byte multiples");
   static_assert(((TX + 4) * sizeof(R)) % 16 == 0, "TMA box rows must be 16-byte multiples");
@@ -316,7 +342,7 @@ __device__ __forceinline__ void fused_finish_cta(const InstanceDesc* __restrict_
 template <class R, int TX, int TY, int NT, int MINB, bool GEN>
 __global__ void __launch_bounds__(NT, MINB)
 k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc) {
-  using S = FusedSmem<R, TX, TY, NT>;
+  using S = FusedSmem<R, TX, TY, NT, MINB>;
   constexpr int NBUF = S::NBUF, PX = S::PX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations
@@ -331,7 +357,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S::bar_off);
   int& s_item = *reinterpret_cast<int*>(smem + S::misc_off);
   int& s_abort = *reinterpret_cast<int*>(smem + S::misc_off + 4);
-  int& s_aitem = *reinterpret_cast<int*>(smem + S::misc_off + 8);  // next phase-A warp item
+  int* s_aitem = reinterpret_cast<int*>(smem + S::misc_off + 8);  // next phase-A warp item, by plane parity
 
   const int tid = threadIdx.x;
   const int ninst = (int)lc->ninst, total = (int)lc->total_items;
@@ -340,7 +366,8 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     for (int s = 0; s < NBUF; s++) mbar_init(&bars[s], 1);
     fence_mbar_init();
     s_abort = 0;
-    s_aitem = 0;
+    s_aitem[0] = 0;
+    s_aitem[1] = 0;
   }
   __syncthreads();
 
@@ -404,8 +431,10 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     };
     auto PV = [&](const R* pl, int n, int i, int j) -> R { return pl[((j + 2) * NPRIM + n) * PX + (i + 2)]; };
     auto PV0 = [&](const R* pl, int i, int j) -> const R& { return pl[((j + 2) * NPRIM) * PX + (i + 2)]; };
-    auto SLX = [&](int n, int i, int j) -> R& { return slx[(n * TY + j) * (TX + 2) + (i + 1)]; };
-    auto SLY = [&](int n, int i, int j) -> R& { return sly[(n * (TY + 2) + (j + 1)) * TX + i]; };
+    R* slxk = slx;  // the x and y slope buffers of the current plane (by plane parity with OV)
+    R* slyk = sly;
+    auto SLX = [&](int n, int i, int j) -> R& { return slxk[(n * TY + j) * (TX + 2) + (i + 1)]; };
+    auto SLY = [&](int n, int i, int j) -> R& { return slyk[(n * (TY + 2) + (j + 1)) * TX + i]; };
     auto SLZ = [&](int b, int n, int i, int j) -> R& { return slz[((b * NPRIM + n) * TY + j) * TX + i]; };
     auto FXS = [&](int m, int i, int j) -> R& { return fxs[(m * TY + j) * (TX + 1) + i]; };
     auto FYS = [&](int m, int i, int j) -> R& { return fys[(m * (TY + 1) + j) * TX + i]; };
@@ -413,6 +442,8 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
 
     // prologue: planes kb-2 .. kb+1 (ke >= kb+1 so all exist)
     if (tid == 0) {
+      s_aitem[0] = 0;
+      s_aitem[1] = 0;
       fence_proxy_async();
       for (int p = kb - 2; p < kb + 2; p++) issue(p);
     }
@@ -422,18 +453,20 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     __syncthreads();
     if (s_abort) break;
 
-    // z slopes of planes kb-1 (buffer 2) and kb (buffer 0).  The flux through face kb-1/2 is formed
-    // in the first plane's phase B by the same code as every other z face, so a face shared by two
-    // chunks comes out bit for bit the same in both (the result cannot depend on the z-chunking).
+    // z slopes of planes kb-1 and kb.  The flux through face kb-1/2 is formed in the first plane's
+    // phase B by the same code as every other z face, so a face shared by two chunks comes out bit
+    // for bit the same in both (the result cannot depend on the z-chunking).  The z slopes of plane
+    // p live in slz buffer (p - kb + 1) % 3, tracked as zc, zn, zf = the buffers of planes k, k+1 and
+    // k+2 (= k-1).
     R fz_lo[NCONS];  // flux through face k-1/2 of the owner's column
-    int zb = 0;      // slz buffer holding the z slope of the current plane
+    int zc = 1, zn = 2, zf = 0;
     if (own) {
       const R *pm2 = plane(kb - 2), *pm1 = plane(kb - 1), *p0 = plane(kb), *pp1 = plane(kb + 1);
 #pragma unroll
       for (int n = 0; n < NPRIM; n++) {
         const R a2 = PV(pm2, n, oi, oj), a1 = PV(pm1, n, oi, oj), b0 = PV(p0, n, oi, oj), b1 = PV(pp1, n, oi, oj);
-        SLZ(2, n, oi, oj) = van_leer(b0 - a1, a1 - a2);
-        SLZ(0, n, oi, oj) = van_leer(b1 - b0, b0 - a1);
+        SLZ(zf, n, oi, oj) = van_leer(b0 - a1, a1 - a2);
+        SLZ(zc, n, oi, oj) = van_leer(b1 - b0, b0 - a1);
       }
     }
     __syncthreads();  // plane kb-2 retired (kb-1 stays until the first plane's faces are formed)
@@ -453,9 +486,18 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
     // does not read, and phase C reads no ring plane, so neither the start nor the end of a plane
     // needs a barrier; the ring slot of plane k is reloaded once phase B has read it.
     // Phase A hands out whole-warp items from a shared counter: the warps without a cell (no phase
-    // C) start on the slopes at once and the owner warps join when their cells are done.
+    // C) start on the slopes at once and the owner warps join when their cells are done.  With OV
+    // the barrier after phase B is a named one that only the owner warps wait at: the others arrive
+    // and go on to the next plane's slopes (into the other x/y slope buffer and the z-slope buffer
+    // that plane k-1's faces read) while the owners' and other warps' last faces are formed.  On the
+    // first plane of a chunk everyone waits, and again after the owners have taken the flux through
+    // face kb-1/2, whose buffer the next plane's z slopes reuse.
     const int nwa = (pxs + pys + pzs) >> 5;
     for (int k = kb; k < ke; k++) {
+      if constexpr (S::OV) {
+        slxk = slx + (k & 1) * (size_t)S::NSLX;
+        slyk = sly + (k & 1) * (size_t)S::NSLY;
+      }
       if (own) {  // the cell's U is read in phase C, two phases from now: pull it into L2
         const double* u0 = a.U + L.at(NCONS, 0, k + NGH, jj + NGH, ii + NGH);
 #pragma unroll
@@ -466,7 +508,7 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       // ---- phase A: slopes ----
       for (;;) {
         int w = 0;
-        if ((tid & 31) == 0) w = atomicAdd(&s_aitem, 1);
+        if ((tid & 31) == 0) w = atomicAdd(&s_aitem[k & 1], 1);
         w = __shfl_sync(0xffffffffu, w, 0);
         if (w >= nwa) break;
         const int q = (w << 5) | (tid & 31);
@@ -496,11 +538,13 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
 #pragma unroll
             for (int n = 0; n < NPRIM; n++) {
               const R c0 = PV(pk, n, i, j), c1 = PV(pk1, n, i, j), c2 = PV(pk2, n, i, j);
-              SLZ(zb ^ 1, n, i, j) = van_leer(c2 - c1, c1 - c0);
+              SLZ(zn, n, i, j) = van_leer(c2 - c1, c1 - c0);
             }
           }
         }
       }
+      // the next plane's counter (last used by plane k-1's phase A, which every warp has left)
+      if (tid == 0) s_aitem[(k + 1) & 1] = 0;
       __syncthreads();
       if (s_abort) break;  // a plane that never arrived (bounded wait): the data above is not used
       // ---- phase B: face fluxes (on the first plane also the faces kb-1/2, into slope buffer 2) ----
@@ -509,7 +553,6 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       // order (normal, first and second tangential components), forms the flux with the
       // direction-generic code (Dir<0>) and stores it back into the unrotated slots.  Only the
       // last warp of the list has idle lanes.
-      if (tid == 0) s_aitem = 0;  // every warp has left phase A; the barrier after phase B publishes it
       const int nfb = nxf + nyf + (k == kb ? 2 * nzf : nzf);
       for (int q = tid; q < ((nfb + 31) & ~31); q += NT) {
         if (q < nfb) {
@@ -544,11 +587,11 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
             rot = 2;
             pa = &PV0(lower ? plane(kb - 1) : pk, i, j);
             pb = &PV0(lower ? pk : pk1, i, j);
-            sa = &SLZ(lower ? 2 : zb, 0, i, j);
-            sb = &SLZ(lower ? zb : (zb ^ 1), 0, i, j);
+            sa = &SLZ(lower ? zf : zc, 0, i, j);
+            sb = &SLZ(lower ? zc : zn, 0, i, j);
             sstr = TY * TX;
             // the lower face overwrites the slopes it alone read (column (i, j) of buffer 2)
-            fo = lower ? &SLZ(2, 0, i, j) : &FZS(0, i, j);
+            fo = lower ? &SLZ(zf, 0, i, j) : &FZS(0, i, j);
             fstr = TY * TX;
           }
           const int c1 = unrot_comp(1, rot), c2 = unrot_comp(2, rot);
@@ -577,7 +620,20 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
           for (int m = 0; m < NCONS; m++) fo[slot_of_flux(m) * fstr] = f[m];
         }
       }
-      __syncthreads();  // faces formed; plane k (and on the first plane kb-1) read for the last time
+      // faces formed; plane k (and on the first plane kb-1) read for the last time
+      if (k == kb) {
+        __syncthreads();
+        if (own) {
+#pragma unroll
+          for (int m = 0; m < NCONS; m++) fz_lo[m] = SLZ(zf, m, oi, oj);
+        }
+        __syncthreads();  // zf now takes plane kb+2's z slopes
+      } else if constexpr (S::OV) {
+        if (tid < S::NOWN) named_bar_sync(1, NT);
+        else named_bar_arrive(1, NT);
+      } else {
+        __syncthreads();
+      }
       if (k == kb && kb + 3 <= ke + 1) {  // plane kb-1's slot
         if (tid == 0) {
           fence_proxy_async();
@@ -594,10 +650,6 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
       }
       // ---- phase C: cell update, recovery, ghost images, candidates ----
       if (own) {
-        if (k == kb) {
-#pragma unroll
-          for (int m = 0; m < NCONS; m++) fz_lo[m] = SLZ(2, m, oi, oj);
-        }
         DivAcc<R> acc;
         const R xi = inv_of<R>(a, 0, ii + NGH);
         const R yi = inv_of<R>(a, 1, (a.quirk ? ii : jj) + NGH);
@@ -632,7 +684,10 @@ k_fused_step(const InstanceDesc* __restrict__ desc, LaunchCtrl* __restrict__ lc)
           cmax = smax(cmax, chc);
         }
       }
-      zb ^= 1;
+      const int z0 = zc;
+      zc = zn;
+      zn = zf;
+      zf = z0;
     }
     if (bad) atomicOr(&ctrl->status, bad);
     block_reduce_to_slot((double)cmin, (double)cmax, red, next);
@@ -704,7 +759,7 @@ __global__ void k_recover(FusedArgs a, int which, RedSlot* slot, const double* _
 // Host side of one instantiation of the fused kernel.
 template <class R, int TX, int TY, int NT, int MINB = 1, bool GEN = false>
 struct FusedLauncher {
-  using S = FusedSmem<R, TX, TY, NT>;
+  using S = FusedSmem<R, TX, TY, NT, MINB>;
   static FusedShape shape() { return FusedShape{TX, TY, S::total, NT, (int)sizeof(R), MINB}; }
   static cudaError_t prepare() {
     return cudaFuncSetAttribute(k_fused_step<R, TX, TY, NT, MINB, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
