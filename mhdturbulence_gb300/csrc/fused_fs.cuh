@@ -41,6 +41,7 @@ struct FusedSmemFS {
   static_assert(NT % 32 == 0 && NT >= TX * TY, "one owner thread per column, whole warps");
   static_assert((TX * sizeof(R)) % 16 == 0, "TMA x offsets must be 16-byte multiples");
   static_assert(((TX + 4) * sizeof(R)) % 16 == 0, "TMA box rows must be 16-byte multiples");
+  static_assert((PLANE * sizeof(R)) % 128 == 0, "each ring slot is a TMA destination: 128-byte aligned");
   static_assert(total <= 227 * 1024, "shared memory budget");
 };
 
