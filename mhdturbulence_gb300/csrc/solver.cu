@@ -17,6 +17,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <numeric>
 #include <string>
 #include <thread>
 #include <tuple>
@@ -610,8 +611,9 @@ std::vector<int> choose_chunks(const Layout& L, int tx, int ty, int ntx, int nty
 }
 
 // Make variant idx the one in use: kernel attribute, grid, work decomposition, tensor maps.
-// kc_fixed > 0 cuts z into chunks of kc_fixed planes (ensembles keep items of similar size across
-// their grids); otherwise the chunking with the best simulated balance is taken (choose_chunks).
+// kc_fixed > 0 cuts z into equal chunks of at most kc_fixed planes (ensembles, whose queue is
+// ordered by item length across their grids); otherwise the chunking with the best simulated
+// balance is taken (choose_chunks).
 int use_variant(mhdgb_solver* h, int idx, int kc_fixed = 0) {
   if (idx < 0 || idx > h->nvars) return fail(h, MHDGB_ERR_ARG, "no such variant");
   const FusedVariant& v = h->vars[idx];
@@ -627,7 +629,8 @@ int use_variant(mhdgb_solver* h, int idx, int kc_fixed = 0) {
   h->nty = (L.ny + h->shape.ty - 1) / h->shape.ty;
   std::vector<int> chunks;
   if (kc_fixed > 0) {
-    const int kc = std::max(std::min(kc_fixed, L.nz), (L.nz + MAX_ZCHUNKS - 1) / MAX_ZCHUNKS);
+    const int nc = std::min((L.nz + kc_fixed - 1) / kc_fixed, MAX_ZCHUNKS);
+    const int kc = (L.nz + nc - 1) / nc;
     for (int k = 0; k < L.nz; k += kc) chunks.push_back(std::min(kc, L.nz - k));
   } else {
     chunks = choose_chunks(L, h->shape.tx, h->shape.ty, h->ntx, h->nty, h->grid);
@@ -1579,7 +1582,12 @@ struct mhdgb_ensemble {
   int nvars = 0, vidx = 0, grid = 0;   // vidx: the HLLD tile variant selected
   int active = 0;                      // the kernel launched: vidx, or nvars (run-time solver) when
                                        // a member uses HLLE/HLLC
-  int kc = 8;                       // planes per work item: similar-sized items across grids
+  // Planes per work item (at most; a grid's z is cut into equal chunks).  A chunk's start costs
+  // about half a plane (the ring's prologue, the lower z faces), so long items pay: on the 64-grid
+  // KH ensemble 8 planes gave 6.41 Gcell/s mixed and 0.361 FP64, 24 gave 7.03 / 0.380, 64 gave
+  // 7.19 / 0.381, flat from 32 on.  The queue takes the grids with the longest items first, so it
+  // ends on short ones.
+  int kc = 64;
   InstanceDesc* d_desc = nullptr;
   LaunchCtrl* d_lc = nullptr;
   int total_items = 0;
@@ -1617,15 +1625,23 @@ bool ens_any_general_solver(const mhdgb_ensemble* e) {
 int ens_use_variant(mhdgb_ensemble* e, int idx) {
   if (idx < 0 || idx >= e->nvars) return efail(e, MHDGB_ERR_ARG, "no such variant");
   const int eff = ens_any_general_solver(e) ? e->nvars : idx;
-  std::vector<InstanceDesc> d(e->m.size());
-  int begin = 0;
   for (size_t i = 0; i < e->m.size(); i++) {
     const bool was = e->m[i]->prepared;
     int rc = use_variant(e->m[i], eff, e->kc);
     if (rc) return ens_member_rc(e, (int)i, rc);
     e->m[i]->prepared = was;
-    d[i] = host_desc(e->m[i], begin);
-    begin += d[i].nitems;
+  }
+  // queue order: the grids with the longest items (first chunk, in planes) first
+  std::vector<size_t> order(e->m.size());
+  std::iota(order.begin(), order.end(), size_t(0));
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return e->m[x]->kst[1] > e->m[y]->kst[1]; });
+  std::vector<InstanceDesc> d;
+  d.reserve(e->m.size());
+  int begin = 0;
+  for (size_t i : order) {
+    d.push_back(host_desc(e->m[i], begin));
+    begin += d.back().nitems;
   }
   e->desc_seen.resize(e->m.size());
   for (size_t i = 0; i < e->m.size(); i++) e->desc_seen[i] = e->m[i]->desc_version;

@@ -144,7 +144,7 @@ def test_work_queue_chunks_cover_the_grid():
             ntx, nty, chunks = s.work_layout()
             assert sum(chunks) == n and min(chunks) >= 1 and len(chunks) <= 64, (n, precision, chunks)
             assert ntx * 16 >= n and nty * 8 >= n
-    # same state with the grid's own chunking and with an ensemble's uniform 8-plane chunks
+    # same state with the grid's own chunking and with an ensemble's equal chunks
     specs = [{"nx": 48, "ny": 40, "nz": 45, "mach": 0.4, "bx": 0.1, "seed": 1}]
     with Ensemble(specs, precision="fp64") as ens, Solver(48, 40, 45, precision="fp64") as s:
         ens.init_kh()
