@@ -557,9 +557,11 @@ double tile_plane_cost(int cx, int cy, int tx, int ty) {
 
 // Finish time of the slowest of `grid` CTAs that take the work items in queue order (chunk-major,
 // then tile rows, then tiles), each CTA the next item when it finishes its last.  A chunk's start
-// costs about kOverheadPlanes planes more (prologue loads, the extra z faces of its first plane).
+// costs about kOverheadPlanes planes more (prologue loads, the extra z faces of its first plane);
+// 1.2 fits the measured times of KH ensembles with 8- to 64-plane items and of eleven chunkings of
+// a 150^3 grid in both forms.
 double simulate_queue(const std::vector<double>& tile_cost, const std::vector<int>& chunks, int grid) {
-  constexpr double kOverheadPlanes = 0.6;
+  constexpr double kOverheadPlanes = 1.2;
   std::vector<double> heap(grid, 0.0);  // min-heap of CTA finish times
   auto cmp = [](double a, double b) { return a > b; };
   for (int c : chunks)
@@ -572,8 +574,9 @@ double simulate_queue(const std::vector<double>& tile_cost, const std::vector<in
 }
 
 // z chunks of a grid for a persistent launch of `grid` CTAs: among uniform chunkings and chunkings
-// whose sizes shrink (each chunk about remaining * tiles / (K * grid) planes, so the queue ends on
-// small items that fill the CTAs' last gaps), the one with the earliest simulated finish.
+// whose sizes shrink (each chunk about remaining * tiles / (K * grid) planes, or a few chunks each
+// a factor r shorter than the one before, so the queue ends on small items that fill the CTAs'
+// last gaps), the one with the earliest simulated finish.
 std::vector<int> choose_chunks(const Layout& L, int tx, int ty, int ntx, int nty, int grid) {
   std::vector<double> cost;
   for (int by = 0; by < nty; by++)
@@ -600,6 +603,17 @@ std::vector<int> choose_chunks(const Layout& L, int tx, int ty, int ntx, int nty
         rem -= s;
       }
       if ((int)c.size() <= MAX_ZCHUNKS) cand.push_back(c);
+    }
+  for (int m = 2; m <= 7 && m <= nz; m++)
+    for (double r : {1.5, 2.0, 2.5, 3.0, 4.0}) {
+      std::vector<double> w(m);
+      double tot = 0.0;
+      for (int i = 0; i < m; i++) tot += (w[i] = std::pow(r, -i));
+      std::vector<int> c(m);
+      int sum = 0;
+      for (int i = 0; i < m; i++) sum += (c[i] = std::max(1, (int)std::lround(nz * w[i] / tot)));
+      c[0] += nz - sum;
+      if (c[0] >= 1) cand.push_back(c);
     }
   double best = 1e300;
   std::vector<int> pick{nz};
