@@ -194,6 +194,12 @@ const char* mhdgb_variant_name(const mhdgb_solver* h, int idx);
  * queue hands out chunk 0 of every tile first; chunks that shrink towards the end of the queue even
  * out the CTAs' finish times. */
 int mhdgb_work_layout(const mhdgb_solver* h, int* ntx, int* nty, int* nchunks, int* kstart);
+/* The z chunking that the fused step plans for an nx x ny x nz grid cut into tx x ty tiles, on a
+ * persistent launch of ctas CTAs: the host-side planner that mhdgb_work_layout reports the result
+ * of (uniform, shrinking and geometric chunkings; the one whose simulated work queue finishes
+ * first).  Writes the chunk lengths in planes (they sum to nz) to chunks[0 .. max_chunks) and
+ * returns their number, or MHDGB_ERR_ARG for a bad size or too small an array.  Needs no device. */
+int mhdgb_plan_zchunks(int nx, int ny, int nz, int tx, int ty, int ctas, int* chunks, int max_chunks);
 /* Time every compiled tile shape on the handle's grid (steps fused steps each, from the current
  * state, which is restored afterwards) and keep the fastest.  The choice is remembered per
  * (precision, nx, ny, nz) for later handles in the process and, if the environment variable

@@ -91,6 +91,8 @@ SIGNATURES = {
                                     C.POINTER(C.c_int)]),
     "mhdgb_select_variant": (C.c_int, [_vp, C.c_int]),
     "mhdgb_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int)]),
+    "mhdgb_plan_zchunks": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                     C.c_int]),
     "mhdgb_measure_fp64_rate": (C.c_int, [C.c_int, _dp]),
     "mhdgb_selftest_division": (C.c_int, [C.c_int, C.c_int, C.c_ulonglong, _dp]),
     "mhdgb_selftest_wait_timeout": (C.c_int, [C.c_int, _dp, C.POINTER(C.c_uint)]),

@@ -1405,6 +1405,18 @@ int mhdgb_work_layout(const mhdgb_solver* h, int* ntx, int* nty, int* nchunks, i
   return MHDGB_OK;
 }
 
+int mhdgb_plan_zchunks(int nx, int ny, int nz, int tx, int ty, int ctas, int* chunks, int max_chunks) {
+  if (nx < 1 || ny < 1 || nz < 1 || tx < 1 || ty < 1 || ctas < 1 || !chunks || max_chunks < 1) return MHDGB_ERR_ARG;
+  Layout L{};
+  L.nx = nx;
+  L.ny = ny;
+  L.nz = nz;
+  const std::vector<int> c = choose_chunks(L, tx, ty, (nx + tx - 1) / tx, (ny + ty - 1) / ty, ctas);
+  if ((int)c.size() > max_chunks) return MHDGB_ERR_ARG;
+  for (size_t i = 0; i < c.size(); i++) chunks[i] = c[i];
+  return (int)c.size();
+}
+
 const char* mhdgb_variant_name(const mhdgb_solver* h, int idx) {
   if (!h) return nullptr;
   if (idx == -1) idx = h->vidx;

@@ -59,3 +59,28 @@ def test_create_rejects_bad_config_before_touching_a_device(libm):
 def test_status_strings(libm):
     for code in range(-7, 1):
         assert libm.mhdgb_status_string(code)
+
+
+def test_z_chunk_planner(libm):
+    """The host-side z-chunk planner of the fused step's work queue: chunks cover every plane once,
+    stay within the kernel's chunk table, and at the benchmark sizes are the chunkings the measured
+    runs used (16x8 tiles; 304 CTAs for the mixed form, 152 for FP64)."""
+    def plan(n, ctas, nz=None):
+        buf = (C.c_int * 64)()
+        k = libm.mhdgb_plan_zchunks(n, n, nz or n, 16, 8, ctas, buf, 64)
+        assert k > 0, (n, ctas, k)
+        return list(buf[:k])
+
+    assert plan(150, 304) == [91, 36, 15, 6, 2]
+    assert plan(150, 152) == [91, 36, 15, 6, 2]
+    assert plan(256, 304) == [216, 34, 6]
+    assert plan(512, 304) == [384, 128]
+    for n in (2, 9, 33, 64, 97, 150, 257, 512, 1000):
+        for ctas in (152, 304):
+            for nz in (n, 3, 2 * n + 1):
+                c = plan(n, ctas, nz)
+                assert sum(c) == nz and min(c) >= 1 and len(c) <= 64, (n, ctas, nz, c)
+    small = (C.c_int * 2)()
+    assert libm.mhdgb_plan_zchunks(150, 150, 150, 16, 8, 304, small, 2) == -1  # needs 5 entries
+    for bad in ((0, 8, 8, 16, 8, 152), (8, 8, 8, 0, 8, 152), (8, 8, 8, 16, 8, 0)):
+        assert libm.mhdgb_plan_zchunks(*bad, small, 2) == -1
